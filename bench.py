@@ -1,0 +1,387 @@
+"""Benchmark of the statevector hot path: the 30-qubit complex<double> layered random circuit
+(depth 60, Toffoli/CCZ at 5% of positions, seed 1) on one GB300.
+
+A step applies one layer of the circuit (its 1-qubit gates, CNOT matching and inserted 3-qubit gates,
+about 47 gates) to the 30-qubit register resident in HBM; steps walk through the circuit's 60 layers.
+`value` is gates/s over the K timed steps (whole job: the sum over ranks' gates / the slowest rank's
+time).  `e2e` repeats the steps through the C ABI from host gate records with a device->host read of a
+qubit probability after every step.  The state (16 GiB) is larger than L2, so no flush is needed.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+--impl reference times the CPU oracle (a restatement of QCSim's QubitRegister loops, OpenMP on all
+host threads) on the same workload, a bounded number of gates per step.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "30q circuit gates/s & HBM frac; fused FP32 vs plain FP64 time @1-F≤1e-6"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=30)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--qubits", type=int, default=30)
+    ap.add_argument("--depth", type=int, default=60)
+    ap.add_argument("--seed", type=int, default=1)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cpu-gates", type=int, default=6, help="gates per CPU step / sample")
+    return ap.parse_args()
+
+
+def peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def algorithmic_bytes(gate, n: int, amp_bytes: int = 16) -> float:
+    """2 * s * 2^n * f(g), f = fraction of rows of the gate matrix that differ from the identity row"""
+    m = gate.getRawOperatorMatrix()
+    d = m.shape[0]
+    changed = sum(1 for r in range(d) if not np.array_equal(m[r], np.eye(d)[r]))
+    return 2.0 * amp_bytes * (2 ** n) * changed / d
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled every 200 ms while running"""
+
+    FIELDS = "clocks.sm,clocks.max.sm,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown," \
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown," \
+             "clocks_event_reasons.sw_power_cap"
+
+    def __init__(self, index: int = 0):
+        self.index = index
+        self.proc = None
+        self.lines: list[str] = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [x.strip() for x in ln.split(",")]
+            if len(parts) < 7:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx.append(float(parts[1]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[3:7]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def dist_init(args):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+        return rank, world, local, dist
+    return rank, world, local, None
+
+
+def barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+def max_over_ranks(dist, v: float) -> float:
+    if dist is None:
+        return v
+    import torch
+    t = torch.tensor([v], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def layers_of(ops, n):
+    """split the layered circuit into its layers (a layer ends with its last CNOT and any 3-qubit gate
+    inserted after it)"""
+    layers, cur, seen_cx = [], [], 0
+    per_layer_cx = n // 2
+    for op in ops:
+        cur.append(op)
+        if type(op[0]).__name__ == "CNOTGate":
+            seen_cx += 1
+        if seen_cx == per_layer_cx:
+            layers.append(cur)
+            cur, seen_cx = [], 0
+    if cur:
+        layers[-1].extend(cur)
+    return layers
+
+
+def cpu_baseline(args, ops, rank):
+    """the CPU oracle on a bounded sample of the workload: the first `cpu_gates` gates at the full size"""
+    from oracle import bind
+    bind.build_oracle()
+    lib = bind.oracle()
+    threads = os.cpu_count() or 1
+    lib.qo_set_threads(threads)
+    n = args.qubits
+    need = 2 * 16 * (2 ** n)
+    avail = 0
+    try:
+        for ln in open("/proc/meminfo"):
+            if ln.startswith("MemAvailable"):
+                avail = int(ln.split()[1]) * 1024
+    except OSError:
+        pass
+    while n > 20 and need > 0.6 * avail:
+        n -= 1
+        need //= 2
+    reg = bind.OracleRegister(n)
+    sample = [op for op in ops if max(op[1:1 + op[0].getQubitsNumber()]) < n][: args.cpu_gates]
+    reg.apply(sample[:1])  # warm-up (first touch)
+    t0 = time.perf_counter()
+    reg.apply(sample)
+    dt = time.perf_counter() - t0
+    gps = len(sample) / dt
+    scaled = gps * (2 ** n) / (2 ** args.qubits)
+    return {"value": scaled, "unit": "gates/s", "cores": lib.qo_max_threads(), "kind": "port",
+            "sample": f"first {len(sample)} gates of the circuit on a {n}-qubit register, {dt:.2f} s"
+                      + ("" if n == args.qubits else f", scaled by 2^{n - args.qubits} to {args.qubits} qubits")}
+
+
+def run_reference(args):
+    rank, world, local, dist = dist_init(args)
+    if rank != 0:
+        return
+    from qcsim_gb300 import circuits
+    from oracle import bind
+    bind.build_oracle()
+    lib = bind.oracle()
+    lib.qo_set_threads(os.cpu_count() or 1)
+    n = args.qubits
+    ops = circuits.layered_circuit(n, args.depth, seed=args.seed, p3=0.05)
+    reg = bind.OracleRegister(n)
+    g = max(1, args.cpu_gates // 3)
+    pos = 0
+    for _ in range(args.warmup):
+        reg.apply(ops[pos:pos + g])
+        pos += g
+    t0 = time.perf_counter()
+    done = 0
+    for _ in range(args.steps):
+        chunk = ops[pos % len(ops):pos % len(ops) + g]
+        reg.apply(chunk)
+        done += len(chunk)
+        pos += g
+    dt = time.perf_counter() - t0
+    v = done / dt
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "gates/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * dt / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": f"layered random circuit, {n} qubits, depth {args.depth}, Toffoli/CCZ at 5%, "
+                                   f"seed {args.seed}; {g} gates per step", "qubits": n},
+            "cpu_baseline": {"value": v, "unit": "gates/s", "cores": lib.qo_max_threads(), "kind": "port",
+                             "sample": f"{g} gates per step, {args.steps} timed steps on the full {n}-qubit register"},
+            "e2e": {"value": v, "unit": "gates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def run_gb300(args):
+    rank, world, local, dist = dist_init(args)
+    import torch
+    torch.cuda.set_device(local)
+    import qcsim_gb300 as Q
+    from qcsim_gb300 import _lib as L, circuits, gates as G
+
+    lib = L.load()
+    n = args.qubits
+    ops = circuits.layered_circuit(n, args.depth, seed=args.seed, p3=0.05)
+    layers = layers_of(ops, n)
+    recs = [G.records(lay) for lay in layers]
+    bytes_layer = [sum(algorithmic_bytes(op[0], n) for op in lay) for lay in layers]
+
+    stream = torch.cuda.Stream()
+    reg = Q.QubitRegister(n, seed=args.seed)
+    lib.qcs_set_stream(reg.handle, stream.cuda_stream)
+
+    def step(i):
+        reg.apply_records(recs[i % len(recs)])
+
+    # warm-up
+    for i in range(args.warmup):
+        step(i)
+    torch.cuda.synchronize()
+
+    # timed region (device time, events on the engine's stream)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    launches0 = lib.qcs_launch_count()
+    with ClockSampler(local) as clk:
+        barrier(dist)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        gates = 0
+        alg_bytes = 0.0
+        for i in range(args.warmup, args.warmup + args.steps):
+            step(i)
+            gates += len(layers[i % len(layers)])
+            alg_bytes += bytes_layer[i % len(layers)]
+        e1.record(stream)
+        torch.cuda.synchronize()
+        barrier(dist)
+    launches = lib.qcs_launch_count() - launches0
+    ms = e0.elapsed_time(e1)
+    ms_max = max_over_ranks(dist, ms)
+    value = gates * world / (ms_max / 1e3)
+    peak, peak_kind = peaks()
+    hbm_frac = alg_bytes / (ms / 1e3) / (peak * 1e9)
+
+    # end to end through the C ABI: host gate records in, a qubit probability out, every step
+    barrier(dist)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    h2d = 0
+    for i in range(args.warmup, args.warmup + args.steps):
+        r = recs[i % len(recs)]
+        reg.apply_records(r)
+        h2d += r.nbytes
+        reg.GetQubitProbability(i % n)
+    torch.cuda.synchronize()
+    e2e_s = max_over_ranks(dist, time.perf_counter() - t0)
+    e2e = {"value": gates * world / e2e_s, "unit": "gates/s", "h2d_bytes_per_step": h2d / args.steps,
+           "d2h_bytes_per_step": 8}
+
+    # dominant kernel: every gate of one layer timed alone (same stream), grouped by kernel family
+    fam_time: dict[str, list] = {}
+    fam_bytes: dict[str, float] = {}
+    lay = layers[1]
+    for rep in range(3):
+        for op in lay:
+            rec = G.records([op])
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            reg.apply_records(rec)
+            b.record(stream)
+            b.synchronize()
+            fam = family(op[0])
+            fam_time.setdefault(fam, []).append(a.elapsed_time(b))
+            fam_bytes[fam] = algorithmic_bytes(op[0], n)
+    shares = {f: sum(v) for f, v in fam_time.items()}
+    dom = max(shares, key=shares.get)
+    dom_ms = statistics.mean(fam_time[dom])
+    achieved = fam_bytes[dom] / (dom_ms / 1e3) / 1e9
+    traffic = read_traffic(dom)
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                "traffic": traffic, "kernel": dom, "peak_source": peak_kind,
+                "algorithmic_bytes_per_launch": fam_bytes[dom], "avg_launch_ms": dom_ms,
+                "share_of_layer_time": shares[dom] / sum(shares.values())}
+
+    # QFT over all qubits, device-timed, one call (its time does not depend on the amplitudes, so the
+    # circuit's output state serves as the input; QFT parity on random normal inputs is in the tests)
+    extra = {}
+    if rank == 0:
+        torch.cuda.synchronize()
+        qops = circuits.qft_circuit(0, n - 1)
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        lib.qcs_qft(reg.handle, 0, n - 1, 0, 1)
+        b.record(stream)
+        b.synchronize()
+        qft_ms = a.elapsed_time(b)
+        qb = sum(algorithmic_bytes(op[0], n) for op in qops)
+        extra["qft"] = {"qubits": n, "seconds": qft_ms / 1e3, "gates": len(qops), "gates_per_s": len(qops) / (qft_ms / 1e3),
+                        "hbm_frac_per_gate": qb / (qft_ms / 1e3) / (peak * 1e9)}
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        cpu = cpu_baseline(args, ops, rank)
+
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": "gates/s", "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+                "config": {"workload": f"layered random circuit, {n} qubits complex<double> (16 GiB), depth "
+                                       f"{args.depth}, Toffoli/CCZ at 5% of positions, seed {args.seed}; one layer "
+                                       "per step", "qubits": n, "gates_timed": gates, "parallelism": f"replicas{world}",
+                           "l2": "state (16 GiB) larger than L2"},
+                "hbm_frac_per_gate": hbm_frac, "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
+                "clocks": clk.summary(), "gpu_launches": int(launches), **extra}
+        print(json.dumps(line))
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+def family(gate) -> str:
+    name = type(gate).__name__
+    return {"HadamardGate": "ctrl1q_real", "RyGate": "ctrl1q_real", "RxGate": "ctrl1q_rxlike", "RzGate": "ctrl1q_diag",
+            "CNOTGate": "ctrl1q_swap", "ToffoliGate": "ctrl1q_swap_cc", "CCZGate": "ctrl1q_phaseneg_cc"}.get(name, name)
+
+
+def read_traffic(kernel_family: str):
+    """DRAM bytes per launch from the committed ncu summary (profiles/*.md, a line
+    'traffic <family> <bytes>'), or None"""
+    for p in sorted((ROOT / "profiles").glob("*.md")):
+        for ln in p.read_text().splitlines():
+            parts = ln.strip().strip("|").split()
+            if len(parts) >= 3 and parts[0] == "traffic" and parts[1] == kernel_family:
+                try:
+                    return float(parts[2])
+                except ValueError:
+                    pass
+    return None
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gb300(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,162 @@
+/*
+ * qcs_gpu.h — C ABI of the GB300 statevector engine (libqcs_gpu.so).
+ *
+ * The engine replaces the statevector hot path of QCSim: QC::QubitRegister (QCSim/QubitRegister.h)
+ * and the static gate/measurement loops of QC::QubitRegisterCalculator
+ * (QCSim/QubitRegisterCalculator.h).  Each entry point below names the reference member it
+ * replaces.  Plain pointers and sizes only; no C++ or CUDA types cross the boundary.
+ *
+ * Conventions
+ *  - A register of n qubits holds 2^n amplitudes; bit q of a basis-state index is qubit q
+ *    (QubitRegister.h:7).  Amplitudes are complex<double> (re, im interleaved, 16 bytes) in
+ *    QCS_FP64 registers and complex<float> in QCS_FP32 registers; host buffers are always
+ *    complex<double>.
+ *  - Gate matrices are 2^k x 2^k complex, row-major, (re, im) interleaved: m[2*(r*2^k + c)].
+ *    Row/column bit 0 is `q0` (the target), bit 1 is `q1` (controllingQubit1) and bit 2 is `q2`
+ *    (controllingQubit2), as in SimpleGates.h:329 and :430.
+ *  - Gate traits are the answers of the gate object's virtuals (SimpleGates.h:27-60), captured by the
+ *    caller; the engine dispatches on them exactly as QubitRegister::ApplyGate does
+ *    (QubitRegister.h:434-486), so only the matrix entries that the reference reads are used.
+ *  - Measurement randomness stays with the caller: each sampling call takes `prob` values, which the
+ *    reference computes as 1 - uniform(rng) (QubitRegister.h:171, 210, 267, 621, 707).
+ *  - Every call is ordered on the register's CUDA stream.  Calls that return values to the host
+ *    synchronise that stream.  A handle is not thread-safe (same as the reference object).
+ *  - Errors: a non-zero status; qcs_last_error(h) gives the message.  For invalid qubit arguments
+ *    the messages are those of QubitRegister::CheckQubits (QubitRegister.h:677-690).
+ */
+#ifndef QCS_GPU_H
+#define QCS_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct qcs_register* qcs_handle;
+
+enum qcs_status {
+	QCS_OK = 0,
+	QCS_INVALID_ARGUMENT = 1, /* reference: std::invalid_argument from CheckQubits */
+	QCS_OUT_OF_MEMORY = 2,
+	QCS_CUDA_ERROR = 3,
+	QCS_UNSUPPORTED = 4
+};
+
+enum qcs_precision { QCS_FP64 = 0, QCS_FP32 = 1 };
+
+/* trait bits: QuantumGate::isDiagonal, isAntidiagonal, isSwapGate, IsISwapGate, IsISwapDagGate,
+ * isControlled and isControlQubit(1) (SimpleGates.h:27-60) */
+enum qcs_trait {
+	QCS_TRAIT_DIAGONAL = 1,
+	QCS_TRAIT_ANTIDIAGONAL = 2,
+	QCS_TRAIT_SWAP = 4,
+	QCS_TRAIT_ISWAP = 8,
+	QCS_TRAIT_ISWAPDAG = 16,
+	QCS_TRAIT_CONTROLLED = 32,
+	QCS_TRAIT_CONTROLQ1 = 64
+};
+
+/* one gate application: ApplyGate(gate, q0, q1, q2) (QubitRegister.h:434) */
+typedef struct qcs_gate {
+	uint32_t k;        /* gate qubits: 1, 2 or 3 */
+	uint32_t q0;       /* qubit */
+	uint32_t q1;       /* controllingQubit1 (ignored when k == 1) */
+	uint32_t q2;       /* controllingQubit2 (ignored when k < 3) */
+	uint32_t traits;   /* qcs_trait bits */
+	uint32_t reserved; /* must be 0 */
+	double m[128];     /* 2^k x 2^k complex matrix, row-major interleaved */
+} qcs_gate;
+
+/* ---- lifetime (QubitRegister ctor QubitRegister.h:17-37, Clone :662-674) ---- */
+/* allocates 2^n amplitudes on the current CUDA device, set to basis state 0 */
+int qcs_create(uint32_t nqubits, int precision, qcs_handle* out);
+int qcs_destroy(qcs_handle h);
+/* copies state, saved state and qubit count into a new register (Clone, QubitRegister.h:662-674) */
+int qcs_clone(qcs_handle h, qcs_handle* out);
+/* orders this register's work on `cuda_stream` (a cudaStream_t; NULL = the engine's own stream) */
+int qcs_set_stream(qcs_handle h, void* cuda_stream);
+int qcs_synchronize(qcs_handle h);
+const char* qcs_last_error(qcs_handle h);
+const char* qcs_status_string(int status);
+uint32_t qcs_nqubits(qcs_handle h);                 /* getNrQubits, QubitRegister.h:59 */
+uint64_t qcs_nstates(qcs_handle h);                 /* getNrBasisStates, QubitRegister.h:60 */
+int qcs_precision_of(qcs_handle h);
+/* device pointer of the amplitude array (for callers that bring their own kernels) */
+void* qcs_device_state(qcs_handle h);
+
+/* ---- state setters (QubitRegister.h:74-122) ---- */
+int qcs_set_basis(qcs_handle h, uint64_t state);     /* setToBasisState :74-80 (out of range: no-op) */
+int qcs_set_qubit_state(qcs_handle h, uint64_t q);   /* setToQubitState :82-88 */
+int qcs_set_cat(qcs_handle h);                       /* setToCatState :91-98 */
+int qcs_set_equal(qcs_handle h);                     /* setToEqualSuperposition :106-109 */
+int qcs_clear(qcs_handle h);                         /* Clear :119-122 */
+int qcs_set_amplitude(qcs_handle h, uint64_t state, double re, double im); /* setRawAmplitude :112-117 */
+int qcs_get_amplitude(qcs_handle h, uint64_t state, double* re_im);        /* getBasisStateAmplitude :62-66 (0 if out of range) */
+/* whole vector, host complex<double>[2^n] (getRegisterStorage :507-510, setRegisterStorageFastNoNormalize :521-524) */
+int qcs_get_state(qcs_handle h, double* host_out);
+int qcs_set_state(qcs_handle h, const double* host_in);
+int qcs_normalize(qcs_handle h);                     /* Normalize :124-130 */
+int qcs_adjust_phase_normalize(qcs_handle h);        /* AdjustPhaseAndNormalize :133-167 */
+
+/* ---- gates ---- */
+/* ApplyGate (QubitRegister.h:434-486) with the trait dispatch of QubitRegisterCalculator.h:39-939 */
+int qcs_apply_gate(qcs_handle h, const double* m, uint32_t k, uint32_t q0, uint32_t q1, uint32_t q2, uint32_t traits);
+/* ApplyGates (QubitRegister.h:493-497): applies the list in order, with the same per-gate results;
+ * consecutive gates may share one pass over the amplitudes (staged in shared memory) */
+int qcs_apply_gates(qcs_handle h, const qcs_gate* gates, size_t count);
+/* ApplyOperatorMatrix (QubitRegister.h:499-505): dense 2^n x 2^n operator, row-major interleaved */
+int qcs_apply_operator_matrix(qcs_handle h, const double* m);
+/* QuantumFourierTransform::QFT / IQFT on qubits [start, end] (QuantumFourierTransform.h:35-87) with
+ * the mirror swaps of QubitsSwapper::Swap (QubitsSwapper.h:23-34) when do_swap != 0 */
+int qcs_qft(qcs_handle h, uint32_t start, uint32_t end, int inverse, int do_swap);
+/* OneQubitGateTransform (HadamardTransform.h:9-41): the same 1-qubit gate on every qubit in [start, end] */
+int qcs_one_qubit_transform(qcs_handle h, const double* m, uint32_t traits, uint32_t start, uint32_t end);
+
+/* ---- measurement (QubitRegister.h:169-429, QubitRegisterCalculator.h:948-1254) ---- */
+/* MeasureAll :169-195 — the first state whose running probability reaches prob (the last state if
+ * none), then collapse to it */
+int qcs_measure_all(qcs_handle h, double prob, uint64_t* state_out);
+/* Measure(first, second) / MeasureQubit :198-224 — collapse and renormalise; returns the measured
+ * sub-register value */
+int qcs_measure(qcs_handle h, uint32_t first, uint32_t second, double prob, uint64_t* value_out);
+/* MeasureNoCollapse() :619-642 — the first state whose running probability reaches prob (state 0 if none) */
+int qcs_measure_no_collapse(qcs_handle h, double prob, uint64_t* state_out);
+/* RepeatedMeasure :243-271 — for each prob, the lower_bound in the running-probability table that
+ * stops at the first entry above 1 - epsilon; an index equal to the table size is possible, as in the
+ * reference.  Results are full basis-state indices (callers mask sub-registers). */
+int qcs_sample(qcs_handle h, const double* probs, size_t nshots, uint64_t* states_out);
+/* GetQubitProbability :592-598 */
+int qcs_qubit_probability(qcs_handle h, uint32_t qubit, double* p_out);
+/* |a_i|^2 for all states into a host double[2^n] */
+int qcs_probabilities(qcs_handle h, double* host_out);
+/* stateFidelity :527-534 against a host complex<double>[2^n] vector: |<psi|v>|^2 */
+int qcs_fidelity_host(qcs_handle h, const double* host_state, double* f_out);
+/* <h|other> between two registers of the same size (the product inside stateFidelity / ExpectationValue) */
+int qcs_inner(qcs_handle h, qcs_handle other, double* re_im_out);
+
+/* ---- snapshots (SaveState / RestoreState / RestoreStateDestructive, QubitRegister.h:600-616) ---- */
+int qcs_save_state(qcs_handle h);
+int qcs_restore_state(qcs_handle h);                 /* no-op when nothing was saved */
+int qcs_restore_state_destructive(qcs_handle h);
+/* ExpectationValue (QubitRegister.h:646-660): <psi| G_n..G_1 |psi> for a gate list, state unchanged */
+int qcs_expectation(qcs_handle h, const qcs_gate* gates, size_t count, double* re_im_out);
+
+/* ---- engine statistics ---- */
+/* number of CUDA kernels this library has launched since it was loaded (all registers) */
+uint64_t qcs_launch_count(void);
+
+/* ---- host random stream: std::mt19937_64 + std::uniform_real_distribution<double>(0,1), the
+ * generator and distribution of QubitRegister.h:723-724, for callers without a C++ runtime ---- */
+typedef struct qcs_rng* qcs_rng_handle;
+int qcs_rng_create(uint64_t seed, qcs_rng_handle* out);
+int qcs_rng_destroy(qcs_rng_handle g);
+/* n uniforms in [0, 1) */
+int qcs_rng_uniform(qcs_rng_handle g, double* out, size_t n);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* QCS_GPU_H */

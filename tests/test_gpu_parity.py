@@ -1,0 +1,331 @@
+"""Parity of the GPU engine (libqcs_gpu.so through the C ABI) with the CPU oracle and with QCSim's own
+outputs (tests/golden).  FP64 tolerance: 1e-12 max amplitude error; measurement outcomes identical
+under the same random stream.  FP32 registers: 2e-6 max amplitude error per gate sequence here."""
+import itertools
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-12
+
+
+@pytest.fixture(scope="module")
+def Q():
+    import qcsim_gb300
+    from qcsim_gb300 import _lib
+    try:
+        _lib.load()
+    except _lib.EngineUnavailable as e:
+        pytest.fail(f"engine not built: {e}")
+    return qcsim_gb300
+
+
+def oracle_state(n, ops, init=None):
+    from oracle import bind as B
+    reg = B.OracleRegister(n)
+    if init is not None:
+        reg.set_state(init)
+    reg.apply(ops)
+    return reg.state()
+
+
+def rand_state(n, seed):
+    r = np.random.default_rng(seed)
+    v = r.standard_normal(1 << n) + 1j * r.standard_normal(1 << n)
+    return v / np.linalg.norm(v)
+
+
+def test_every_gate_every_placement(Q):
+    """each gate class on every ordered qubit placement of a 5-qubit register"""
+    from qcsim_gb300 import gates as G
+    n = 5
+    init = rand_state(n, 1)
+    reg = Q.QubitRegister(n, seed=1)
+    worst = 0.0
+    for code in sorted(G.BY_CODE):
+        g = G.make(code, 0.9, -0.4, 1.3, 0.2)
+        k = g.getQubitsNumber()
+        for qs in itertools.permutations(range(n), k):
+            qs = list(qs) + [0] * (3 - k)
+            reg.setRegisterStorageFastNoNormalize(init)
+            reg.ApplyGate(g, *qs)
+            got = reg.getRegisterStorage()
+            want = oracle_state(n, [(g, *qs)], init)
+            worst = max(worst, np.abs(got - want).max())
+            assert np.abs(got - want).max() <= TOL, (code, qs)
+    assert worst <= TOL
+
+
+def test_matrix_only_gates(Q):
+    """AppliedGate (no traits) takes the dense 2x2 / 4x4 / 8x8 paths"""
+    from qcsim_gb300 import gates as G
+    n = 6
+    r = np.random.default_rng(3)
+    init = rand_state(n, 2)
+    reg = Q.QubitRegister(n, seed=1)
+    for k in (1, 2, 3):
+        for qs in list(itertools.permutations(range(n), k))[::3]:
+            a = r.standard_normal((1 << k, 1 << k)) + 1j * r.standard_normal((1 << k, 1 << k))
+            u, _ = np.linalg.qr(a)
+            qs = list(qs) + [0] * (3 - k)
+            g = G.AppliedGate(u, *qs)
+            reg.setRegisterStorageFastNoNormalize(init)
+            reg.ApplyGate(g)
+            assert np.abs(reg.getRegisterStorage() - oracle_state(n, [(g, *qs)], init)).max() <= TOL
+
+
+def test_golden_random_circuits(Q, golden):
+    from test_oracle_golden import split_recs
+    from qcsim_gb300 import _lib as L, gates as G
+    import ctypes as C
+    from oracle import bind as B
+    off = 0
+    for n, recs in split_recs(golden):
+        ref = golden["circ_states"][off:off + (1 << n)]
+        off += 1 << n
+        # rebuild the gate objects from codes/params (the engine gets matrices + traits)
+        ops = []
+        for r in recs:
+            code = int(r["code"])
+            if code >= 50:
+                k = code - 49
+                d = 1 << k
+                m = r["m"][: 2 * d * d].view(np.complex128).reshape(d, d)
+                g = G.AppliedGate(m, int(r["q0"]), int(r["q1"]), int(r["q2"]))
+            else:
+                g = G.make(code, *r["p"])
+            ops.append((g, int(r["q0"]), int(r["q1"]), int(r["q2"])))
+        reg = Q.QubitRegister(n, seed=1)
+        for op in ops:
+            reg.ApplyGate(*op)
+        assert np.abs(reg.getRegisterStorage() - ref).max() <= TOL
+        reg2 = Q.QubitRegister(n, seed=1)
+        reg2.ApplyGates(ops)
+        assert np.abs(reg2.getRegisterStorage() - ref).max() <= TOL
+    _ = (L, C, B)
+
+
+def test_layered_12_golden(Q, golden):
+    from qcsim_gb300 import circuits
+    ops = circuits.layered_circuit(12, 10, seed=4, p3=0.05)
+    reg = Q.QubitRegister(12, seed=7)
+    reg.ApplyGates(ops)
+    assert np.abs(reg.getRegisterStorage() - golden["l12_state"]).max() <= TOL
+    qp = np.array([reg.GetQubitProbability(q) for q in range(12)])
+    assert np.abs(qp - golden["l12_qprob"]).max() <= TOL
+    hist = reg.RepeatedMeasure(1024)
+    assert np.array_equal(np.array(sorted(hist.items()), dtype=np.uint64), golden["l12_hist"])
+    assert reg.MeasureAll() == golden["l12_measure_all"][0]
+    st = reg.getRegisterStorage()
+    assert st[int(golden["l12_measure_all"][0])] == 1 and np.count_nonzero(st) == 1
+
+
+@pytest.mark.parametrize("seed", [1, 2, 3])
+def test_layered_20_parity(Q, golden, seed):
+    """the 20-qubit layered workload (depth 40): full state vs the oracle, probe amplitudes, qubit
+    probabilities and 1024 seeded shots vs the reference"""
+    from qcsim_gb300 import circuits
+    ops = circuits.layered_circuit(20, 40, seed=seed)
+    reg = Q.QubitRegister(20, seed=seed)
+    reg.ApplyGates(ops)
+    st = reg.getRegisterStorage()
+    assert np.abs(st - oracle_state(20, ops)).max() <= TOL
+    assert np.abs(st[golden["c0_probe_idx"]] - golden["c0_amp"][seed - 1]).max() <= TOL
+    qp = np.array([reg.GetQubitProbability(q) for q in range(20)])
+    assert np.abs(qp - golden["c0_qprob"][seed - 1]).max() <= 1e-12
+    off = int(np.sum(golden["c0_hist_len"][: seed - 1]))
+    want = golden["c0_hist"][off:off + golden["c0_hist_len"][seed - 1]]
+    got = np.array(sorted(reg.RepeatedMeasure(1024).items()), dtype=np.uint64)
+    assert np.array_equal(got, want)
+
+
+def test_measurement_kats(Q, golden):
+    for (s, op, v), after in zip(golden["kat_rows"], golden["kat_after"]):
+        reg = Q.QubitRegister(2, seed=1000 + int(s))
+        reg.setToBasisState(0)
+        reg.setRawAmplitude(0, 0.5)
+        reg.setRawAmplitude(1, -0.5j)
+        reg.setRawAmplitude(3, 1 / np.sqrt(2))
+        reg.Normalize()
+        got = [lambda: reg.MeasureQubit(0), lambda: reg.MeasureQubit(1), lambda: reg.Measure(0, 1),
+               reg.MeasureAll, reg.MeasureNoCollapse][int(op)]()
+        assert got == v
+        assert np.abs(reg.getRegisterStorage() - after).max() <= 1e-15
+
+
+def test_subregister_measurements(Q, golden):
+    for (a, b, v), after in zip(golden["sub_rows"], golden["sub_after"]):
+        a, b = int(a), int(b)
+        reg = Q.QubitRegister(10, seed=31 + a * 10 + b)
+        reg.setRegisterStorageFastNoNormalize(golden["sub_state"])
+        assert reg.Measure(a, b) == v
+        assert np.abs(reg.getRegisterStorage() - after).max() <= 1e-14
+    for a, b in ((0, 0), (3, 5), (2, 9), (9, 9), (0, 9)):
+        rows = golden["sub_hist"][(golden["sub_hist"][:, 0] == a) & (golden["sub_hist"][:, 1] == b)]
+        reg = Q.QubitRegister(10, seed=77 + a * 10 + b)
+        reg.setRegisterStorageFastNoNormalize(golden["sub_state"])
+        h = reg.RepeatedMeasure(a, b, 500)
+        assert np.array_equal(np.array(sorted(h.items()), dtype=np.uint64), rows[:, 2:])
+
+
+def test_scan_edges(Q, golden):
+    for row in golden["edge_rows"]:
+        s = int(row[0])
+        reg = Q.QubitRegister(10, seed=500 + s)
+        reg.setRegisterStorageFastNoNormalize(golden["edge_state"])
+        assert reg.MeasureNoCollapse() == row[2]
+        h = reg.RepeatedMeasure(64)
+        assert np.array_equal(np.array([k for k in sorted(h) for _ in range(h[k])], dtype=np.uint64), row[3:])
+        reg.setRegisterStorageFastNoNormalize(golden["edge_state"])
+        assert reg.MeasureAll() == row[1]
+
+
+def test_qft(Q, golden):
+    from qcsim_gb300 import algorithms
+    for cfg, inp, outp in zip(golden["qft_cfg"], golden["qft_in"], golden["qft_out"]):
+        n, s0, e0, inv, sw = (int(x) for x in cfg)
+        reg = Q.QubitRegister(n, seed=1)
+        reg.setRegisterStorageFastNoNormalize(inp[: 1 << n])
+        qft = algorithms.QuantumFourierTransform(n, s0, e0)
+        (qft.IQFT if inv else qft.QFT)(reg, bool(sw))
+        assert np.abs(reg.getRegisterStorage() - outp[: 1 << n]).max() <= TOL
+
+
+@pytest.mark.parametrize("n", [12, 18])
+def test_qft_random_state(Q, n):
+    from qcsim_gb300 import algorithms, circuits
+    v = circuits.random_normal_state(n, 5)
+    reg = Q.QubitRegister(n, seed=1)
+    reg.setRegisterStorageFastNoNormalize(v)
+    algorithms.QuantumFourierTransform(n).QFT(reg)
+    want = oracle_state(n, circuits.qft_circuit(0, n - 1), v)
+    assert np.abs(reg.getRegisterStorage() - want).max() <= TOL
+    # QFT then IQFT returns the input
+    algorithms.QuantumFourierTransform(n).IQFT(reg)
+    assert np.abs(reg.getRegisterStorage() - v).max() <= 1e-11
+
+
+def test_qaoa(Q, golden):
+    from qcsim_gb300 import circuits
+    insts = circuits.qaoa_instances(4, seed=8, nmin=6, nmax=10, p=2)
+    for inst, st, en in zip(insts, golden["qaoa_states"], golden["qaoa_energy"]):
+        n = inst["n"]
+        reg = Q.QubitRegister(n, seed=1)
+        reg.ApplyGates(circuits.qaoa_circuit(inst))
+        got = reg.getRegisterStorage()
+        assert np.abs(got - st[: 1 << n]).max() <= TOL
+        e_exact = float(np.dot(reg.probabilities(), en[: 1 << n]))
+        assert abs(e_exact - float(np.dot(np.abs(st[: 1 << n]) ** 2, en[: 1 << n]))) <= 1e-12
+
+
+def test_expectation_and_replay(Q, golden):
+    from qcsim_gb300 import gates as G
+    from test_gpu_parity import _ops_from_recs
+    ops = _ops_from_recs(golden["exp_recs"])
+    pre = _ops_from_recs(golden["exp_pre"])
+    reg = Q.QubitRegister(6, seed=1)
+    reg.ApplyGates(ops)
+    v = reg.ExpectationValue([g for (g, *_) in pre])
+    assert abs(v - complex(*golden["exp_value"])) <= 1e-13
+    assert np.abs(reg.getRegisterStorage() - golden["exp_state_after"]).max() <= TOL
+    assert reg.ExpectationValue([]) == 1.0
+    for mode, want in ((1, golden["replay_states"][0]), (2, golden["replay_states"][1])):
+        r2 = Q.QubitRegister(6, seed=1)
+        r2.ComputeStart()
+        for op in ops:
+            r2.ApplyGate(*op)
+        r2.ComputeEnd()
+        (r2.Compute if mode == 1 else r2.Uncompute)()
+        assert np.abs(r2.getRegisterStorage() - want).max() <= TOL
+    _ = G
+
+
+def _ops_from_recs(recs):
+    from qcsim_gb300 import gates as G
+    ops = []
+    for r in recs:
+        code = int(r["code"])
+        if code >= 50:
+            d = 1 << (code - 49)
+            g = G.AppliedGate(r["m"][: 2 * d * d].view(np.complex128).reshape(d, d), int(r["q0"]), int(r["q1"]), int(r["q2"]))
+        else:
+            g = G.make(code, *r["p"])
+        ops.append((g, int(r["q0"]), int(r["q1"]), int(r["q2"])))
+    return ops
+
+
+def test_invalid_arguments(Q):
+    from qcsim_gb300 import gates as G
+    reg = Q.QubitRegister(3, seed=1)
+    for args, msg in (((G.HadamardGate(), 3), "Qubit number is too high"),
+                      ((G.CNOTGate(), 1, 1), "Qubit and controlling qubit are the same"),
+                      ((G.CNOTGate(), 1, 5), "Controlling qubit number is too high"),
+                      ((G.ToffoliGate(), 0, 1, 1), "Qubits must be different"),
+                      ((G.ToffoliGate(), 0, 1, 7), "Controlling qubit number is too high")):
+        with pytest.raises(ValueError, match=msg):
+            reg.ApplyGate(*args)
+
+
+def test_state_api(Q):
+    n = 8
+    reg = Q.QubitRegister(n, seed=3)
+    assert reg.getBasisStateAmplitude(0) == 1
+    reg.setToQubitState(3)
+    assert reg.getBasisStateProbability(8) == 1
+    reg.setToQubitState(99)  # out of range: no-op
+    assert reg.getBasisStateProbability(8) == 1
+    reg.setToCatState()
+    st = reg.getRegisterStorage()
+    assert st[0] == st[-1] == 1 / np.sqrt(2)
+    reg.setToEqualSuperposition()
+    assert np.allclose(reg.getRegisterStorage(), 1 / 16)
+    assert reg.getBasisStateAmplitude(1 << n) == 0
+    v = rand_state(n, 9) * 3.0
+    reg.setRegisterStorage(v)
+    assert abs(np.linalg.norm(reg.getRegisterStorage()) - 1) < 1e-14
+    reg.setRegisterStorageFastNoNormalize(v)
+    reg.AdjustPhaseAndNormalize()
+    want = v / v[0]
+    want /= np.linalg.norm(want)
+    assert np.abs(reg.getRegisterStorage() - want).max() < 1e-14
+    assert abs(reg.stateFidelity(want) - 1) < 1e-13
+    reg.SaveState()
+    reg.ApplyGate(Q.gates.HadamardGate(), 2)
+    c = reg.Clone()
+    reg.RestoreState()
+    assert np.abs(reg.getRegisterStorage() - want).max() < 1e-14
+    c.RestoreStateDestructive()
+    assert np.abs(c.getRegisterStorage() - want).max() < 1e-14
+    m = np.linalg.qr(np.random.default_rng(1).standard_normal((256, 256)))[0].astype(np.complex128)
+    reg.ApplyOperatorMatrix(m)
+    assert np.abs(reg.getRegisterStorage() - m @ want).max() < 1e-13
+    reg.Clear()
+    assert not reg.getRegisterStorage().any()
+
+
+def test_fp32_register(Q):
+    from qcsim_gb300 import circuits
+    n = 14
+    ops = circuits.layered_circuit(n, 8, seed=2, p3=0.05)
+    reg = Q.QubitRegister(n, seed=1, precision="fp32")
+    reg.ApplyGates(ops)
+    want = oracle_state(n, ops)
+    got = reg.getRegisterStorage()
+    assert np.abs(got - want).max() < 2e-6
+    assert 1 - abs(np.vdot(want, got)) ** 2 < 1e-9
+
+
+def test_larger_register_properties(Q):
+    """24 qubits: unitary circuits keep the norm; an inverse circuit returns the start state"""
+    from qcsim_gb300 import circuits
+    n = 24
+    ops = circuits.layered_circuit(n, 6, seed=9, p3=0.05)
+    reg = Q.QubitRegister(n, seed=1)
+    reg.ApplyGates(ops)
+    p = reg.probabilities()
+    assert abs(p.sum() - 1) < 1e-12
+    inv =[(type(g)(*(-x for x in g.params()[:1])) if hasattr(g, "theta") else g, *q) for (g, *q) in reversed(ops)]
+    reg.ApplyGates(inv)
+    assert abs(reg.getBasisStateAmplitude(0) - 1) < 1e-11

@@ -1,0 +1,107 @@
+"""Host-side checks that need no GPU: the gate library mirrors the reference's classes, the seeded
+generators are deterministic, and libqcs_gpu.so loads and exports every entry point of
+include/qcs_gpu.h (no compute calls)."""
+import ctypes as C
+import re
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from qcsim_gb300 import _lib as L
+from qcsim_gb300 import circuits, gates as G
+from qcsim_gb300.rng import Mt19937_64
+
+ROOT = Path(__file__).resolve().parents[1]
+
+
+def test_gate_library_matches_reference(golden):
+    p = tuple(golden["gate_params"])
+    for code, m, k, t in zip(golden["gate_codes"], golden["gate_mats"], golden["gate_k"], golden["gate_traits"]):
+        g = G.make(int(code), *p)
+        d = 1 << int(k)
+        assert g.getQubitsNumber() == k
+        assert g.traits() == t, (code, g.traits(), t)
+        got = np.ascontiguousarray(g.getRawOperatorMatrix()).reshape(-1).view(np.float64)
+        assert np.array_equal(got, m[: 2 * d * d]), code
+
+
+def test_gate_records_layout():
+    rec = G.to_record(G.ControlledPhaseShiftGate(0.3), 4, 2)
+    assert rec["k"] == 2 and rec["q0"] == 4 and rec["q1"] == 2
+    assert rec["traits"] == L.TRAIT_CONTROLLED | L.TRAIT_DIAGONAL
+    assert rec["m"][30] == np.cos(0.3) and rec["m"][31] == np.sin(0.3)
+    assert L.GATE_DTYPE.itemsize == 6 * 4 + 128 * 8
+
+
+def test_rng_matches_reference(golden):
+    for row, seed in zip(golden["rng_uniforms"], (1, 7, 123456789)):
+        m = Mt19937_64(seed)
+        assert np.array_equal(np.array([m.uniform() for _ in range(row.size)]), row)
+
+
+def test_layered_generator_shape():
+    ops = circuits.layered_circuit(20, 40, seed=1)
+    assert len(ops) == 40 * (20 + 10)
+    ops2 = circuits.layered_circuit(20, 40, seed=1)
+    assert all(type(a[0]) is type(b[0]) and a[1:] == b[1:] for a, b in zip(ops, ops2))
+    ops3 = circuits.layered_circuit(30, 60, seed=1, p3=0.05)
+    n3 = sum(1 for o in ops3 if o[0].getQubitsNumber() == 3)
+    assert 60 <= n3 <= 230  # about 5% of 2700 positions
+    for o in ops3:
+        assert len(set(o[1:1 + o[0].getQubitsNumber()])) == o[0].getQubitsNumber()
+
+
+def test_qaoa_instances():
+    insts = circuits.qaoa_instances(16, seed=3)
+    for inst in insts:
+        n = inst["n"]
+        assert n % 2 == 0 and 12 <= n <= 24
+        deg = np.zeros(n, dtype=int)
+        for i, j in inst["edges"]:
+            assert i < j
+            deg[i] += 1
+            deg[j] += 1
+        assert np.all(deg == 3)
+        assert len(set(inst["edges"])) == len(inst["edges"])
+
+
+def _declared_symbols():
+    names = set()
+    for h in (ROOT / "include").glob("*.h"):
+        text = h.read_text()
+        text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+        for m in re.finditer(r"^\s*(?:[A-Za-z_][\w\s\*]*?)\b(qcs_\w+)\s*\(", text, flags=re.M):
+            names.add(m.group(1))
+    return names
+
+
+def test_c_abi_exports_every_declared_symbol():
+    lib_path = L.LIB_PATH
+    if not lib_path.exists():
+        pytest.skip("libqcs_gpu.so not built")
+    lib = C.CDLL(str(lib_path))
+    declared = _declared_symbols()
+    assert len(declared) >= 40
+    missing = [n for n in sorted(declared) if not hasattr(lib, n)]
+    assert not missing, missing
+    # the Python binding declares exactly the header's entry points
+    assert declared == set(L.SIGNATURES), declared ^ set(L.SIGNATURES)
+
+
+def test_status_strings_without_gpu():
+    if not L.LIB_PATH.exists():
+        pytest.skip("libqcs_gpu.so not built")
+    lib = L.load()
+    assert lib.qcs_status_string(L.QCS_INVALID_ARGUMENT) == b"invalid argument"
+    # creation fails cleanly (no device here, or an invalid size)
+    h = C.c_void_p()
+    assert lib.qcs_create(0, L.QCS_FP64, C.byref(h)) == L.QCS_INVALID_ARGUMENT
+
+
+def test_engine_rng_matches_reference(golden):
+    if not L.LIB_PATH.exists():
+        pytest.skip("libqcs_gpu.so not built")
+    from qcsim_gb300.register import Rng
+    for row, seed in zip(golden["rng_uniforms"], (1, 7, 123456789)):
+        assert np.array_equal(Rng(seed).uniform(row.size), row)
