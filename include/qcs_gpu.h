@@ -143,6 +143,12 @@ int qcs_restore_state_destructive(qcs_handle h);
 /* ExpectationValue (QubitRegister.h:646-660): <psi| G_n..G_1 |psi> for a gate list, state unchanged */
 int qcs_expectation(qcs_handle h, const qcs_gate* gates, size_t count, double* re_im_out);
 
+/* ---- engine options ---- */
+enum qcs_option {
+	QCS_OPT_PASSES = 1 /* 1 (default): gate lists run as shared-memory passes; 0: one kernel per gate */
+};
+int qcs_set_option(qcs_handle h, int option, int value);
+
 /* ---- engine statistics ---- */
 /* number of CUDA kernels this library has launched since it was loaded (all registers) */
 uint64_t qcs_launch_count(void);

@@ -17,6 +17,7 @@ LIB_PATH = Path(os.environ.get("QCS_GPU_LIB", PKG / "libqcs_gpu.so"))
 
 QCS_OK, QCS_INVALID_ARGUMENT, QCS_OUT_OF_MEMORY, QCS_CUDA_ERROR, QCS_UNSUPPORTED = range(5)
 QCS_FP64, QCS_FP32 = 0, 1
+QCS_OPT_PASSES = 1
 
 TRAIT_DIAGONAL = 1
 TRAIT_ANTIDIAGONAL = 2
@@ -92,6 +93,7 @@ SIGNATURES = {
     "qcs_restore_state": (_i, [_h]),
     "qcs_restore_state_destructive": (_i, [_h]),
     "qcs_expectation": (_i, [_h, C.c_void_p, _sz, _pd]),
+    "qcs_set_option": (_i, [_h, _i, _i]),
     "qcs_launch_count": (_u64, []),
     "qcs_rng_create": (_i, [_u64, C.POINTER(_h)]),
     "qcs_rng_destroy": (_i, [_h]),

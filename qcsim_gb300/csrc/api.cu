@@ -11,6 +11,7 @@
 
 #include "engine.cuh"
 #include "batch.cuh"
+#include "compile.cuh"
 
 using qcs::BitPlan;
 using qcs::DenseArgs;
@@ -41,34 +42,9 @@ int cuda_fail(qcs_handle h, cudaError_t e, const char* where) {
 		if (e_ != cudaSuccess) return cuda_fail((h), e_, where); \
 	} while (0)
 
-cd entry(const double* m, int dim, int r, int c) { return cd(m[2 * (r * dim + c)], m[2 * (r * dim + c) + 1]); }
 
-template <typename T> typename qcs::cplx_t<T> to_c(const cd& v) {
-	typename qcs::cplx_t<T> r;
-	r.x = static_cast<T>(v.real());
-	r.y = static_cast<T>(v.imag());
-	return r;
-}
 
-template <typename T> Mat2<T> mat2(const cd& a, const cd& b, const cd& c, const cd& d) {
-	Mat2<T> m;
-	m.m00 = to_c<T>(a);
-	m.m01 = to_c<T>(b);
-	m.m10 = to_c<T>(c);
-	m.m11 = to_c<T>(d);
-	return m;
-}
 
-BitPlan plan_of(std::initializer_list<uint32_t> qubits, uint64_t set_mask) {
-	BitPlan p;
-	std::vector<int> v;
-	for (uint32_t q : qubits) v.push_back(static_cast<int>(q));
-	std::sort(v.begin(), v.end());
-	p.nins = static_cast<int>(v.size());
-	for (int i = 0; i < p.nins; ++i) p.ins[i] = v[i];
-	p.set_mask = set_mask;
-	return p;
-}
 
 // QubitRegister::CheckQubits (QubitRegister.h:677-690)
 int check_qubits(qcs_handle h, uint32_t k, uint64_t q, uint64_t c1, uint64_t c2) {
@@ -86,112 +62,43 @@ int check_qubits(qcs_handle h, uint32_t k, uint64_t q, uint64_t c1, uint64_t c2)
 	return QCS_OK;
 }
 
-// the 2x2 block the reference reads, as a diagonal: ApplyOneQubitGate's diagonal branch
-// (QubitRegisterCalculator.h:41-52), ApplyDiagonalControlGate (:357-371), ApplyDiagonalCCGate (:642-656)
-template <typename T>
-cudaError_t run_diag(qcs_handle h, const cd& d0, const cd& d1, uint32_t t, BitPlan pl) {
-	auto* s = static_cast<qcs::cplx_t<T>*>(h->d_state);
-	const cd one(1, 0);
-	const uint64_t tbit = 1ULL << t;
-	if (d0 == one && d1 == one) return cudaSuccess;  // identity
-	if (d0 == one || d1 == one) {
-		// only the half whose factor is not one changes
-		const cd f = (d0 == one) ? d1 : d0;
-		const uint64_t which = (d0 == one) ? tbit : 0;
-		Op1 op = Op1::Phase;
-		if (f == cd(-1, 0)) op = Op1::PhaseNeg;
-		else if (f == cd(0, 1) || f == cd(0, -1)) op = Op1::PhaseI;
-		return qcs::launch_ctrl1q<T>(s, h->N, op, mat2<T>(one, 0, 0, f), which, pl, h->sms, h->stream);
-	}
-	return qcs::launch_ctrl1q<T>(s, h->N, Op1::Diag, mat2<T>(d0, 0, 0, d1), tbit, pl, h->sms, h->stream);
+// scale factors taken out of gates are kept on the host and folded into the amplitudes before the
+// state is read, measured or copied (and when their magnitude leaves a safe range)
+int materialize(qcs_handle h) {
+	if (h->scale == cd(1, 0)) return QCS_OK;
+	cudaError_t e = h->prec == QCS_FP64
+	                    ? qcs::launch_scale_complex<double>(static_cast<double2*>(h->d_state), h->N, h->scale.real(), h->scale.imag(), h->sms, h->stream)
+	                    : qcs::launch_scale_complex<float>(static_cast<float2*>(h->d_state), h->N, h->scale.real(), h->scale.imag(), h->sms, h->stream);
+	QCS_CK(h, e, "scale");
+	h->scale = cd(1, 0);
+	return QCS_OK;
 }
 
-// antidiagonal block: ApplyOneQubitGate (:57-67), ApplyAntidiagonalControlGate (:373-393),
-// ApplyAntidiagonalCCGate (:658-680)
-template <typename T>
-cudaError_t run_antidiag(qcs_handle h, const cd& v01, const cd& v10, uint32_t t, BitPlan pl) {
-	auto* s = static_cast<qcs::cplx_t<T>*>(h->d_state);
-	const cd one(1, 0);
-	const Op1 op = (v01 == one && v10 == one) ? Op1::Swap : Op1::Antidiag;
-	return qcs::launch_ctrl1q<T>(s, h->N, op, mat2<T>(0, v01, v10, 0), 1ULL << t, pl, h->sms, h->stream);
-}
-
-// general 2x2 block: ApplyOneQubitGate (:68-79), ApplyGenericControlGate (:395-417),
-// ApplyGenericCCGate (:682-707)
-template <typename T>
-cudaError_t run_general(qcs_handle h, const cd& a, const cd& b, const cd& c, const cd& d, uint32_t t, BitPlan pl) {
-	auto* s = static_cast<qcs::cplx_t<T>*>(h->d_state);
-	Op1 op = Op1::Generic;
-	if (a.imag() == 0 && b.imag() == 0 && c.imag() == 0 && d.imag() == 0) op = Op1::Real;
-	else if (a.imag() == 0 && d.imag() == 0 && b.real() == 0 && c.real() == 0) op = Op1::RxLike;
-	return qcs::launch_ctrl1q<T>(s, h->N, op, mat2<T>(a, b, c, d), 1ULL << t, pl, h->sms, h->stream);
-}
-
-// QubitRegister::ApplyGate (QubitRegister.h:434-486) dispatching like QubitRegisterCalculator's
-// ApplyOneQubitGate / ApplyTwoQubitsGate / ApplyThreeQubitsGate (QubitRegisterCalculator.h:39-227)
-template <typename T>
-cudaError_t dispatch(qcs_handle h, const double* m, uint32_t k, uint32_t q0, uint32_t q1, uint32_t q2, uint32_t tr) {
-	auto* s = static_cast<qcs::cplx_t<T>*>(h->d_state);
-	const int dim = 1 << k;
-	const uint64_t b0 = 1ULL << q0;
-	if (k == 1) {
-		const BitPlan pl = plan_of({q0}, 0);
-		if (tr & QCS_TRAIT_DIAGONAL) return run_diag<T>(h, entry(m, 2, 0, 0), entry(m, 2, 1, 1), q0, pl);
-		if (tr & QCS_TRAIT_ANTIDIAGONAL) return run_antidiag<T>(h, entry(m, 2, 0, 1), entry(m, 2, 1, 0), q0, pl);
-		return run_general<T>(h, entry(m, 2, 0, 0), entry(m, 2, 0, 1), entry(m, 2, 1, 0), entry(m, 2, 1, 1), q0, pl);
+// QubitRegister::ApplyGate (QubitRegister.h:434-486) through the compiled trait dispatch
+cudaError_t dispatch_one(qcs_handle h, const qcs_gate& g) {
+	const qcs::CompiledGate c = qcs::compile_gate(g, true);
+	cudaError_t e = h->prec == QCS_FP64 ? qcs::launch_compiled<double>(static_cast<double2*>(h->d_state), h->N, c, h->sms, h->stream)
+	                                    : qcs::launch_compiled<float>(static_cast<float2*>(h->d_state), h->N, c, h->sms, h->stream);
+	if (e != cudaSuccess) return e;
+	h->scale *= c.scale;
+	const double mag = std::abs(h->scale);
+	if (mag > 1e100 || mag < 1e-100) {
+		if (materialize(h) != QCS_OK) return cudaErrorUnknown;
 	}
-	if (k == 2) {
-		const uint64_t b1 = 1ULL << q1;
-		if (tr & (QCS_TRAIT_SWAP | QCS_TRAIT_ISWAP | QCS_TRAIT_ISWAPDAG)) {
-			const SwapKind kind = (tr & QCS_TRAIT_SWAP) ? SwapKind::Plain : ((tr & QCS_TRAIT_ISWAP) ? SwapKind::ISwap : SwapKind::ISwapDag);
-			return qcs::launch_swap<T>(s, h->N, kind, b1, b0, plan_of({q0, q1}, 0), h->sms, h->stream);
-		}
-		if (tr & QCS_TRAIT_CONTROLLED) {
-			const BitPlan pl = plan_of({q0, q1}, b1);
-			if (tr & QCS_TRAIT_DIAGONAL) return run_diag<T>(h, entry(m, 4, 2, 2), entry(m, 4, 3, 3), q0, pl);
-			if (tr & QCS_TRAIT_ANTIDIAGONAL) return run_antidiag<T>(h, entry(m, 4, 2, 3), entry(m, 4, 3, 2), q0, pl);
-			return run_general<T>(h, entry(m, 4, 2, 2), entry(m, 4, 2, 3), entry(m, 4, 3, 2), entry(m, 4, 3, 3), q0, pl);
-		}
-		DenseArgs a;
-		a.k = 2;
-		a.bit[0] = b0;
-		a.bit[1] = b1;
-		std::memcpy(a.m, m, sizeof(double) * 2 * dim * dim);
-		return qcs::launch_dense<T>(s, h->N, a, plan_of({q0, q1}, 0), h->sms, h->stream);
-	}
-	const uint64_t b1 = 1ULL << q1, b2 = 1ULL << q2;
-	if (tr & QCS_TRAIT_SWAP)  // Fredkin: controllingQubit2 controls the exchange of qubit and controllingQubit1
-		return qcs::launch_swap<T>(s, h->N, SwapKind::Plain, b1, b0, plan_of({q0, q1, q2}, b2), h->sms, h->stream);
-	if (tr & QCS_TRAIT_CONTROLLED) {
-		if (tr & QCS_TRAIT_CONTROLQ1) {
-			const BitPlan pl = plan_of({q0, q1, q2}, b1 | b2);
-			if (tr & QCS_TRAIT_DIAGONAL) return run_diag<T>(h, entry(m, 8, 6, 6), entry(m, 8, 7, 7), q0, pl);
-			if (tr & QCS_TRAIT_ANTIDIAGONAL) return run_antidiag<T>(h, entry(m, 8, 6, 7), entry(m, 8, 7, 6), q0, pl);
-			return run_general<T>(h, entry(m, 8, 6, 6), entry(m, 8, 6, 7), entry(m, 8, 7, 6), entry(m, 8, 7, 7), q0, pl);
-		}
-		// one control (controllingQubit2): the 4x4 block of rows/columns 4..7
-		DenseArgs a;
-		a.k = 2;
-		a.bit[0] = b0;
-		a.bit[1] = b1;
-		for (int r = 0; r < 4; ++r)
-			for (int c = 0; c < 4; ++c) {
-				a.m[2 * (r * 4 + c)] = m[2 * ((4 + r) * 8 + 4 + c)];
-				a.m[2 * (r * 4 + c) + 1] = m[2 * ((4 + r) * 8 + 4 + c) + 1];
-			}
-		return qcs::launch_dense<T>(s, h->N, a, plan_of({q0, q1, q2}, b2), h->sms, h->stream);
-	}
-	DenseArgs a;
-	a.k = 3;
-	a.bit[0] = b0;
-	a.bit[1] = b1;
-	a.bit[2] = b2;
-	std::memcpy(a.m, m, sizeof(double) * 2 * 64);
-	return qcs::launch_dense<T>(s, h->N, a, plan_of({q0, q1, q2}, 0), h->sms, h->stream);
+	return cudaSuccess;
 }
 
 cudaError_t dispatch_any(qcs_handle h, const double* m, uint32_t k, uint32_t q0, uint32_t q1, uint32_t q2, uint32_t tr) {
-	return h->prec == QCS_FP64 ? dispatch<double>(h, m, k, q0, q1, q2, tr) : dispatch<float>(h, m, k, q0, q1, q2, tr);
+	qcs_gate g;
+	g.k = k;
+	g.q0 = q0;
+	g.q1 = q1;
+	g.q2 = q2;
+	g.traits = tr;
+	g.reserved = 0;
+	const int dim = 1 << k;
+	std::memcpy(g.m, m, sizeof(double) * 2 * dim * dim);
+	return dispatch_one(h, g);
 }
 
 int apply_checked(qcs_handle h, const double* m, uint32_t k, uint32_t q0, uint32_t q1, uint32_t q2, uint32_t tr) {
@@ -203,6 +110,7 @@ int apply_checked(qcs_handle h, const double* m, uint32_t k, uint32_t q0, uint32
 
 // sum of |a_i|^2 over (i & mask) == value
 int masked_prob(qcs_handle h, uint64_t mask, uint64_t value, double* out) {
+	if (int st = materialize(h)) return st;
 	cudaError_t e = h->prec == QCS_FP64
 	                    ? qcs::reduce_masked_prob<double>(static_cast<double2*>(h->d_state), h->N, mask, value, h->sc, h->sms, h->stream, out)
 	                    : qcs::reduce_masked_prob<float>(static_cast<float2*>(h->d_state), h->N, mask, value, h->sc, h->sms, h->stream, out);
@@ -219,6 +127,7 @@ int scale_masked(qcs_handle h, uint64_t mask, uint64_t value, double f) {
 }
 
 int sample_any(qcs_handle h, const double* probs, size_t n, int mode, uint64_t fallback, uint64_t* out) {
+	if (int st = materialize(h)) return st;
 	cudaError_t e = h->prec == QCS_FP64
 	                    ? qcs::sample<double>(static_cast<double2*>(h->d_state), h->N, probs, n, mode, fallback, h->sc, h->sms, h->stream, out)
 	                    : qcs::sample<float>(static_cast<float2*>(h->d_state), h->N, probs, n, mode, fallback, h->sc, h->sms, h->stream, out);
@@ -227,6 +136,7 @@ int sample_any(qcs_handle h, const double* probs, size_t n, int mode, uint64_t f
 }
 
 int set_basis_impl(qcs_handle h, uint64_t state) {
+	if (state < h->N) h->scale = cd(1, 0);
 	if (state >= h->N) return QCS_OK;
 	QCS_CK(h, cudaMemsetAsync(h->d_state, 0, h->state_bytes(), h->stream), "clear");
 	cudaError_t e = h->prec == QCS_FP64 ? qcs::launch_set_one<double>(static_cast<double2*>(h->d_state), state, 1.0, 0.0, h->stream)
@@ -236,6 +146,7 @@ int set_basis_impl(qcs_handle h, uint64_t state) {
 }
 
 int read_amp(qcs_handle h, uint64_t idx, cd* out) {
+	if (int st = materialize(h)) return st;
 	if (h->prec == QCS_FP64) {
 		double v[2];
 		QCS_CK(h, cudaMemcpyAsync(v, static_cast<char*>(h->d_state) + idx * 16, 16, cudaMemcpyDeviceToHost, h->stream), "read amplitude");
@@ -333,6 +244,9 @@ int qcs_destroy(qcs_handle h) {
 }
 
 int qcs_clone(qcs_handle h, qcs_handle* out) {
+	if (h) {
+		if (int st = materialize(h)) return st;
+	}
 	if (!h || !out) return QCS_INVALID_ARGUMENT;
 	qcs_handle c = nullptr;
 	int st = qcs_create(h->n, h->prec, &c);
@@ -369,6 +283,15 @@ int qcs_set_stream(qcs_handle h, void* cuda_stream) {
 	return QCS_OK;
 }
 
+int qcs_set_option(qcs_handle h, int option, int value) {
+	if (!h) return QCS_INVALID_ARGUMENT;
+	if (option == QCS_OPT_PASSES) {
+		h->batch_mode = value ? 1 : 0;
+		return QCS_OK;
+	}
+	return fail(h, QCS_INVALID_ARGUMENT, "unknown option");
+}
+
 int qcs_synchronize(qcs_handle h) {
 	if (!h) return QCS_INVALID_ARGUMENT;
 	QCS_CK(h, cudaStreamSynchronize(h->stream), "synchronize");
@@ -393,6 +316,7 @@ int qcs_set_qubit_state(qcs_handle h, uint64_t q) {
 }
 
 int qcs_set_cat(qcs_handle h) {
+	if (h) h->scale = cd(1, 0);
 	if (!h) return QCS_INVALID_ARGUMENT;
 	QCS_CK(h, cudaMemsetAsync(h->d_state, 0, h->state_bytes(), h->stream), "cat");
 	const double v = 1. / std::sqrt(2.);
@@ -409,6 +333,7 @@ int qcs_set_cat(qcs_handle h) {
 }
 
 int qcs_set_equal(qcs_handle h) {
+	if (h) h->scale = cd(1, 0);
 	if (!h) return QCS_INVALID_ARGUMENT;
 	const double v = 1. / std::sqrt(static_cast<double>(h->N));
 	cudaError_t e = h->prec == QCS_FP64 ? qcs::launch_fill_const<double>(static_cast<double2*>(h->d_state), h->N, v, 0, h->stream)
@@ -418,12 +343,16 @@ int qcs_set_equal(qcs_handle h) {
 }
 
 int qcs_clear(qcs_handle h) {
+	if (h) h->scale = cd(1, 0);
 	if (!h) return QCS_INVALID_ARGUMENT;
 	QCS_CK(h, cudaMemsetAsync(h->d_state, 0, h->state_bytes(), h->stream), "clear");
 	return QCS_OK;
 }
 
 int qcs_set_amplitude(qcs_handle h, uint64_t state, double re, double im) {
+	if (h) {
+		if (int st = materialize(h)) return st;
+	}
 	if (!h) return QCS_INVALID_ARGUMENT;
 	if (state >= h->N) return QCS_OK;
 	cudaError_t e = h->prec == QCS_FP64 ? qcs::launch_set_one<double>(static_cast<double2*>(h->d_state), state, re, im, h->stream)
@@ -447,6 +376,9 @@ int qcs_get_amplitude(qcs_handle h, uint64_t state, double* re_im) {
 }
 
 int qcs_get_state(qcs_handle h, double* host_out) {
+	if (h && h->scale != cd(1, 0)) {
+		if (int st = materialize(h)) return st;
+	}
 	if (!h || !host_out) return QCS_INVALID_ARGUMENT;
 	if (h->prec == QCS_FP64) {
 		QCS_CK(h, cudaMemcpyAsync(host_out, h->d_state, h->state_bytes(), cudaMemcpyDeviceToHost, h->stream), "get state");
@@ -469,6 +401,7 @@ int qcs_get_state(qcs_handle h, double* host_out) {
 }
 
 int qcs_set_state(qcs_handle h, const double* host_in) {
+	if (h) h->scale = cd(1, 0);
 	if (!h || !host_in) return QCS_INVALID_ARGUMENT;
 	if (h->prec == QCS_FP64) {
 		QCS_CK(h, cudaMemcpyAsync(h->d_state, host_in, h->state_bytes(), cudaMemcpyHostToDevice, h->stream), "set state");
@@ -531,6 +464,9 @@ int qcs_apply_gates(qcs_handle h, const qcs_gate* gates, size_t count) {
 }
 
 int qcs_apply_operator_matrix(qcs_handle h, const double* m) {
+	if (h) {
+		if (int st = materialize(h)) return st;
+	}
 	if (!h || !m) return QCS_INVALID_ARGUMENT;
 	if (h->n > 13) return fail(h, QCS_UNSUPPORTED, "dense operators are limited to 13 qubits (a 2^n x 2^n matrix)");
 	double2* dM = nullptr;
@@ -615,6 +551,9 @@ int qcs_qubit_probability(qcs_handle h, uint32_t qubit, double* p_out) {
 }
 
 int qcs_probabilities(qcs_handle h, double* host_out) {
+	if (h && h->scale != cd(1, 0)) {
+		if (int st = materialize(h)) return st;
+	}
 	if (!h || !host_out) return QCS_INVALID_ARGUMENT;
 	const uint64_t chunk = std::min<uint64_t>(h->N, kStageAmps);
 	double* tmp = nullptr;
@@ -635,6 +574,9 @@ int qcs_probabilities(qcs_handle h, double* host_out) {
 // stateFidelity (QubitRegister.h:527-534): the host vector is staged in chunks; partial inner
 // products are added in chunk order
 int qcs_fidelity_host(qcs_handle h, const double* host_state, double* f_out) {
+	if (h && h->scale != cd(1, 0)) {
+		if (int st = materialize(h)) return st;
+	}
 	if (!h || !host_state || !f_out) return QCS_INVALID_ARGUMENT;
 	const uint64_t chunk = std::min<uint64_t>(h->N, kStageAmps);
 	double2* tmp = nullptr;
@@ -659,6 +601,10 @@ int qcs_fidelity_host(qcs_handle h, const double* host_state, double* f_out) {
 }
 
 int qcs_inner(qcs_handle h, qcs_handle other, double* re_im_out) {
+	if (h && other) {
+		if (int st = materialize(h)) return st;
+		if (int st = materialize(other)) return st;
+	}
 	if (!h || !other || !re_im_out) return QCS_INVALID_ARGUMENT;
 	if (other->N != h->N || other->prec != h->prec) return fail(h, QCS_INVALID_ARGUMENT, "registers differ in size or precision");
 	QCS_CK(h, cudaStreamSynchronize(other->stream), "inner product");
@@ -670,6 +616,9 @@ int qcs_inner(qcs_handle h, qcs_handle other, double* re_im_out) {
 }
 
 int qcs_save_state(qcs_handle h) {
+	if (h) {
+		if (int st = materialize(h)) return st;
+	}
 	if (!h) return QCS_INVALID_ARGUMENT;
 	if (!h->d_saved) QCS_CK(h, cudaMalloc(&h->d_saved, h->state_bytes()), "save state");
 	QCS_CK(h, cudaMemcpyAsync(h->d_saved, h->d_state, h->state_bytes(), cudaMemcpyDeviceToDevice, h->stream), "save state");
@@ -680,6 +629,7 @@ int qcs_save_state(qcs_handle h) {
 int qcs_restore_state(qcs_handle h) {
 	if (!h) return QCS_INVALID_ARGUMENT;
 	if (!h->has_saved) return QCS_OK;
+	h->scale = cd(1, 0);
 	QCS_CK(h, cudaMemcpyAsync(h->d_state, h->d_saved, h->state_bytes(), cudaMemcpyDeviceToDevice, h->stream), "restore state");
 	return QCS_OK;
 }
@@ -688,6 +638,7 @@ int qcs_restore_state_destructive(qcs_handle h) {
 	if (!h) return QCS_INVALID_ARGUMENT;
 	if (!h->has_saved) return QCS_OK;
 	QCS_CK(h, cudaStreamSynchronize(h->stream), "restore state");
+	h->scale = cd(1, 0);
 	std::swap(h->d_state, h->d_saved);
 	cudaFree(h->d_saved);
 	h->d_saved = nullptr;
@@ -697,6 +648,9 @@ int qcs_restore_state_destructive(qcs_handle h) {
 
 // ExpectationValue (QubitRegister.h:646-660)
 int qcs_expectation(qcs_handle h, const qcs_gate* gates, size_t count, double* re_im_out) {
+	if (h) {
+		if (int st = materialize(h)) return st;
+	}
 	if (!h || !re_im_out || (count && !gates)) return QCS_INVALID_ARGUMENT;
 	if (count == 0) {
 		re_im_out[0] = 1;
@@ -711,6 +665,7 @@ int qcs_expectation(qcs_handle h, const qcs_gate* gates, size_t count, double* r
 		return cuda_fail(h, e, "expectation");
 	}
 	int st = qcs_apply_gates(h, gates, count);
+	if (st == QCS_OK) st = materialize(h);
 	if (st == QCS_OK) {
 		e = h->prec == QCS_FP64
 		        ? qcs::inner_product<double>(static_cast<double2*>(copy), static_cast<double2*>(h->d_state), h->N, h->sc, h->sms, h->stream, re_im_out)
@@ -756,7 +711,8 @@ void note_launches(uint64_t n) { g_launches.fetch_add(n, std::memory_order_relax
 
 extern "C" uint64_t qcs_launch_count(void) { return qcs::g_launches.load(); }
 
-// exported for the batch planner: one gate through the per-gate kernels
+// exported for the batch planner: one gate through the per-gate kernels, and the scale fold
 namespace qcs {
-cudaError_t apply_one(qcs_handle h, const qcs_gate& g) { return dispatch_any(h, g.m, g.k, g.q0, g.q1, g.q2, g.traits); }
+cudaError_t apply_one(qcs_handle h, const qcs_gate& g) { return dispatch_one(h, g); }
+int fold_scale(qcs_handle h) { return materialize(h); }
 }  // namespace qcs

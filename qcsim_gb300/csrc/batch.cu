@@ -1,10 +1,18 @@
 // Gate-list execution (ApplyGates, QubitRegister.h:493-497) and the QFT gate sequence
 // (QuantumFourierTransform.h:35-87, QubitsSwapper.h:23-34).
+//
+// The planner walks the gate list in order and packs consecutive gates into shared-memory passes:
+// a gate joins the open pass when the qubits it must hold locally (targets of non-diagonal blocks;
+// controls and diagonal targets never need to be local) fit in the pass's tile.  Every gate keeps its
+// own arithmetic and order, so results equal those of the per-gate kernels.
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <vector>
 
 #include "batch.cuh"
+#include "compile.cuh"
+#include "tile.cuh"
 
 namespace qcs {
 namespace {
@@ -44,17 +52,201 @@ qcs_gate make_swap(uint32_t a, uint32_t b) {
 	return g;
 }
 
+struct PlannedPass {
+	uint64_t tmask = 0;
+	std::vector<CompiledGate> gates;
+	std::complex<double> fold_after{1.0, 0.0};  // scale folded into the amplitudes after this pass
+};
+
+int popcount64(uint64_t x) { return __builtin_popcountll(x); }
+
+// device buffers of the planner, per register
+struct BatchBuffers {
+	void* d_ops = nullptr;
+	size_t ops_cap = 0;
+	void* d_mats = nullptr;
+	size_t mats_cap = 0;
+};
+
+cudaError_t ensure(void** p, size_t* cap, size_t bytes) {
+	if (*cap >= bytes) return cudaSuccess;
+	if (*p) cudaFree(*p);
+	*p = nullptr;
+	*cap = 0;
+	cudaError_t e = cudaMalloc(p, bytes);
+	if (e == cudaSuccess) *cap = bytes;
+	return e;
+}
+
+template <typename T> void push_mat2(std::vector<cplx_t<T>>& mats, const Mat2<double>& m) {
+	const double2 v[4] = {m.m00, m.m01, m.m10, m.m11};
+	for (const double2& x : v) {
+		cplx_t<T> c;
+		c.x = static_cast<T>(x.x);
+		c.y = static_cast<T>(x.y);
+		mats.push_back(c);
+	}
+}
+
+template <typename T>
+int run_planned(qcs_handle h, const std::vector<PlannedPass>& passes, int kmax, int L0) {
+	const int n = static_cast<int>(h->n);
+	std::vector<TilePass> tps;
+	std::vector<TileOp> ops;
+	std::vector<cplx_t<T>> mats;
+	for (const PlannedPass& pp : passes) {
+		// tile qubits: the required ones, completed from the bottom up to kmax
+		uint64_t T_ = pp.tmask | ((1ULL << L0) - 1);
+		for (int q = 0; q < n && popcount64(T_) < kmax; ++q) T_ |= 1ULL << q;
+		TilePass tp;
+		std::memset(&tp, 0, sizeof(tp));
+		tp.k = popcount64(T_);
+		int L = 0;
+		while (L < n && ((T_ >> L) & 1ULL)) ++L;
+		tp.L = L;
+		int lpos[64];
+		int nh = 0;
+		for (int q = 0; q < n; ++q) {
+			if (!((T_ >> q) & 1ULL)) continue;
+			if (q < L) lpos[q] = q;
+			else {
+				lpos[q] = L + nh;
+				tp.high[nh++] = static_cast<uint8_t>(q);
+			}
+		}
+		int nf = 0;
+		for (int q = 0; q < n; ++q)
+			if (!((T_ >> q) & 1ULL)) tp.fixed[nf++] = static_cast<uint8_t>(q);
+		tp.nfixed = nf;
+		tp.op_begin = static_cast<uint32_t>(ops.size());
+		for (const CompiledGate& c : pp.gates) {
+			TileOp op;
+			std::memset(&op, 0, sizeof(op));
+			std::vector<int> ins;
+			for (uint32_t i = 0; i < c.ncontrols; ++i) {
+				const uint32_t q = c.controls[i];
+				if ((T_ >> q) & 1ULL) {
+					op.lset |= 1u << lpos[q];
+					ins.push_back(lpos[q]);
+				} else {
+					op.gmask |= 1ULL << q;
+				}
+			}
+			op.mat = static_cast<uint32_t>(mats.size());
+			if (c.kind == GKind::Ctrl1q) {
+				op.op = static_cast<uint8_t>(c.op);
+				push_mat2<T>(mats, c.m);
+				if ((T_ >> c.target) & 1ULL) {
+					op.kind = static_cast<uint8_t>(TKind::Ctrl1q);
+					ins.push_back(lpos[c.target]);
+					op.lbit0 = c.phase_on_a0 ? 0u : (1u << lpos[c.target]);
+				} else {
+					op.kind = static_cast<uint8_t>(TKind::GlobalDiag);
+					op.gtbit = 1ULL << c.target;
+					op.lbit0 = c.phase_on_a0 ? 0u : 1u;
+				}
+			} else if (c.kind == GKind::Swap) {
+				op.kind = static_cast<uint8_t>(TKind::Swap);
+				op.op = static_cast<uint8_t>(c.sk);
+				ins.push_back(lpos[c.qa]);
+				ins.push_back(lpos[c.qb]);
+				op.lbit0 = 1u << lpos[c.qa];
+				op.lbit1 = 1u << lpos[c.qb];
+			} else if (c.kind == GKind::Dense) {
+				op.kind = static_cast<uint8_t>(c.dense_k == 2 ? TKind::Dense2 : TKind::Dense3);
+				const uint32_t lb[3] = {c.dense_k > 0 ? 1u << lpos[c.dense_q[0]] : 0u, c.dense_k > 1 ? 1u << lpos[c.dense_q[1]] : 0u,
+				                        c.dense_k > 2 ? 1u << lpos[c.dense_q[2]] : 0u};
+				op.lbit0 = lb[0];
+				op.lbit1 = lb[1];
+				op.lbit2 = lb[2];
+				for (int j = 0; j < c.dense_k; ++j) ins.push_back(lpos[c.dense_q[j]]);
+				const int D = 1 << c.dense_k;
+				for (int i = 0; i < D * D; ++i) {
+					cplx_t<T> v;
+					v.x = static_cast<T>(c.dense_m[2 * i]);
+					v.y = static_cast<T>(c.dense_m[2 * i + 1]);
+					mats.push_back(v);
+				}
+			} else {
+				continue;
+			}
+			std::sort(ins.begin(), ins.end());
+			op.nins = static_cast<uint8_t>(ins.size());
+			for (size_t i = 0; i < ins.size(); ++i) op.ins |= static_cast<uint32_t>(ins[i]) << (8 * i);
+			ops.push_back(op);
+		}
+		tp.op_count = static_cast<uint32_t>(ops.size()) - tp.op_begin;
+		tps.push_back(tp);
+	}
+	BatchBuffers* bb = static_cast<BatchBuffers*>(h->batch);
+	if (!bb) {
+		bb = new BatchBuffers;
+		h->batch = bb;
+	}
+	cudaError_t e = ensure(&bb->d_ops, &bb->ops_cap, std::max<size_t>(1, ops.size()) * sizeof(TileOp));
+	if (e == cudaSuccess) e = ensure(&bb->d_mats, &bb->mats_cap, std::max<size_t>(1, mats.size()) * sizeof(cplx_t<T>));
+	if (e == cudaSuccess && !ops.empty())
+		e = cudaMemcpyAsync(bb->d_ops, ops.data(), ops.size() * sizeof(TileOp), cudaMemcpyHostToDevice, h->stream);
+	if (e == cudaSuccess && !mats.empty())
+		e = cudaMemcpyAsync(bb->d_mats, mats.data(), mats.size() * sizeof(cplx_t<T>), cudaMemcpyHostToDevice, h->stream);
+	auto* s = static_cast<cplx_t<T>*>(h->d_state);
+	for (size_t i = 0; i < tps.size() && e == cudaSuccess; ++i) {
+		if (tps[i].op_count > 0)
+			e = launch_tile_pass<T>(s, tps[i], static_cast<const TileOp*>(bb->d_ops), static_cast<const cplx_t<T>*>(bb->d_mats), h->sms, h->stream);
+		const std::complex<double> f = passes[i].fold_after;
+		if (e == cudaSuccess && f != std::complex<double>(1.0, 0.0))
+			e = launch_scale_complex<T>(s, h->N, f.real(), f.imag(), h->sms, h->stream);
+	}
+	// the host vectors must outlive the (pageable, stream-ordered) copies
+	if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+	if (e != cudaSuccess) {
+		h->err = std::string("apply gates: ") + cudaGetErrorString(e);
+		return QCS_CUDA_ERROR;
+	}
+	return QCS_OK;
+}
+
 }  // namespace
 
 int batch_apply(qcs_handle h, const qcs_gate* gates, size_t count) {
+	const int n = static_cast<int>(h->n);
+	const int kmax = h->prec == QCS_FP64 ? tile_qubits<double>() : tile_qubits<float>();
+	if (n < kmax + 2 || count < 2 || h->batch_mode == 0) {
+		for (size_t i = 0; i < count; ++i) {
+			cudaError_t e = apply_one(h, gates[i]);
+			if (e != cudaSuccess) {
+				h->err = std::string("apply gates: ") + cudaGetErrorString(e);
+				return QCS_CUDA_ERROR;
+			}
+		}
+		return QCS_OK;
+	}
+	const int L0 = std::max(5, kmax - 8);
+	std::vector<PlannedPass> passes(1);
+	passes.back().tmask = (1ULL << L0) - 1;
 	for (size_t i = 0; i < count; ++i) {
-		cudaError_t e = apply_one(h, gates[i]);
-		if (e != cudaSuccess) {
-			h->err = std::string("apply gates: ") + cudaGetErrorString(e);
-			return QCS_CUDA_ERROR;
+		CompiledGate c = compile_gate(gates[i], true);
+		h->scale *= c.scale;
+		const double mag = std::abs(h->scale);
+		if (c.kind != GKind::Identity) {
+			const uint64_t need = c.local_mask();
+			PlannedPass& cur = passes.back();
+			if (popcount64(cur.tmask | need) > kmax) {
+				passes.emplace_back();
+				passes.back().tmask = ((1ULL << L0) - 1) | need;
+			} else {
+				cur.tmask |= need;
+			}
+			passes.back().gates.push_back(c);
+		}
+		if (mag > 1e100 || mag < 1e-100) {
+			passes.back().fold_after = h->scale;
+			h->scale = std::complex<double>(1.0, 0.0);
+			passes.emplace_back();
+			passes.back().tmask = (1ULL << L0) - 1;
 		}
 	}
-	return QCS_OK;
+	return h->prec == QCS_FP64 ? run_planned<double>(h, passes, kmax, L0) : run_planned<float>(h, passes, kmax, L0);
 }
 
 std::vector<qcs_gate> qft_gates(uint32_t start, uint32_t end, bool inverse, bool do_swap) {
@@ -95,6 +287,13 @@ int qft_apply(qcs_handle h, uint32_t start, uint32_t end, bool inverse, bool do_
 	return batch_apply(h, gs.data(), gs.size());
 }
 
-void batch_release(qcs_handle) {}
+void batch_release(qcs_handle h) {
+	BatchBuffers* bb = static_cast<BatchBuffers*>(h->batch);
+	if (!bb) return;
+	if (bb->d_ops) cudaFree(bb->d_ops);
+	if (bb->d_mats) cudaFree(bb->d_mats);
+	delete bb;
+	h->batch = nullptr;
+}
 
 }  // namespace qcs

@@ -3,6 +3,7 @@
 
 #include <cuda_runtime.h>
 #include <cstdint>
+#include <complex>
 #include <cstddef>
 #include <string>
 
@@ -32,7 +33,12 @@ enum class Op1 : int {
 	Swap,            // (a0, a1) <- (a1, a0)
 	Real,            // real 2x2
 	RxLike,          // real diagonal, imaginary off-diagonal
-	Generic          // complex 2x2
+	Generic,         // complex 2x2
+	AntidiagUnit,    // (a0, a1) <- (u01 a1, u10 a0), u in {1, i, -1, -i}
+	UnitRe01,        // factored rotations: one +-1 entry per row, the other real or imaginary
+	UnitRe10,
+	UnitIm01,
+	UnitIm10
 };
 
 enum class SwapKind : int { Plain = 0, ISwap, ISwapDag };
@@ -82,6 +88,9 @@ struct qcs_register {
 	int device = 0;
 	int sms = 148;
 	qcs::Scratch sc;
+	std::complex<double> scale{1.0, 0.0};  // amplitudes = scale * stored values
+	void* batch = nullptr;                 // planner buffers (batch.cu)
+	int batch_mode = 1;                    // QCS_OPT_PASSES
 	std::string err;
 	size_t amp_bytes() const { return prec == QCS_FP64 ? 16 : 8; }
 	size_t state_bytes() const { return static_cast<size_t>(N) * amp_bytes(); }

@@ -8,69 +8,10 @@
 //
 // Semantics follow QCSim's QubitRegisterCalculator loops (cited per kernel); the reference's
 // out-of-place copies of untouched amplitudes become "leave in place".
-#include "engine.cuh"
+#include "gate_math.cuh"
 
 namespace qcs {
 namespace {
-
-template <typename T> __device__ __forceinline__ cplx_t<T> mk(T x, T y) { cplx_t<T> r; r.x = x; r.y = y; return r; }
-
-template <typename T> __device__ __forceinline__ cplx_t<T> cmul(const cplx_t<T>& a, const cplx_t<T>& b) {
-	return mk<T>(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
-}
-
-template <int NINS> __device__ __forceinline__ uint64_t expand(uint64_t p, const BitPlan& pl) {
-#pragma unroll
-	for (int j = 0; j < NINS; ++j) {
-		const int b = pl.ins[j];
-		p = ((p >> b) << (b + 1)) | (p & ((1ULL << b) - 1));
-	}
-	return p | pl.set_mask;
-}
-
-// the 2x2 arithmetic of each Op1 (QubitRegisterCalculator.h:39-135 for one qubit, :357-417 for the
-// controlled block, :642-707 for the double-controlled block)
-template <typename T, Op1 OP>
-__device__ __forceinline__ void op2(cplx_t<T>& a0, cplx_t<T>& a1, const Mat2<T>& m) {
-	if constexpr (OP == Op1::Diag) {
-		a0 = cmul<T>(a0, m.m00);
-		a1 = cmul<T>(a1, m.m11);
-	} else if constexpr (OP == Op1::Phase) {
-		a1 = cmul<T>(a1, m.m11);
-	} else if constexpr (OP == Op1::PhaseNeg) {
-		a1 = mk<T>(-a1.x, -a1.y);
-	} else if constexpr (OP == Op1::PhaseI) {
-		// (x + iy) * (i*s) = -s*y + i*s*x
-		const T sgn = m.m11.y;
-		a1 = mk<T>(-sgn * a1.y, sgn * a1.x);
-	} else if constexpr (OP == Op1::Antidiag) {
-		const cplx_t<T> n0 = cmul<T>(m.m01, a1);
-		a1 = cmul<T>(m.m10, a0);
-		a0 = n0;
-	} else if constexpr (OP == Op1::Swap) {
-		const cplx_t<T> t = a0;
-		a0 = a1;
-		a1 = t;
-	} else if constexpr (OP == Op1::Real) {
-		const cplx_t<T> n0 = mk<T>(m.m00.x * a0.x + m.m01.x * a1.x, m.m00.x * a0.y + m.m01.x * a1.y);
-		a1 = mk<T>(m.m10.x * a0.x + m.m11.x * a1.x, m.m10.x * a0.y + m.m11.x * a1.y);
-		a0 = n0;
-	} else if constexpr (OP == Op1::RxLike) {
-		const cplx_t<T> n0 = mk<T>(m.m00.x * a0.x - m.m01.y * a1.y, m.m00.x * a0.y + m.m01.y * a1.x);
-		a1 = mk<T>(m.m11.x * a1.x - m.m10.y * a0.y, m.m11.x * a1.y + m.m10.y * a0.x);
-		a0 = n0;
-	} else {
-		const cplx_t<T> n0 = mk<T>(m.m00.x * a0.x - m.m00.y * a0.y + m.m01.x * a1.x - m.m01.y * a1.y,
-		                           m.m00.x * a0.y + m.m00.y * a0.x + m.m01.x * a1.y + m.m01.y * a1.x);
-		a1 = mk<T>(m.m10.x * a0.x - m.m10.y * a0.y + m.m11.x * a1.x - m.m11.y * a1.y,
-		           m.m10.x * a0.y + m.m10.y * a0.x + m.m11.x * a1.y + m.m11.y * a1.x);
-		a0 = n0;
-	}
-}
-
-template <Op1 OP> constexpr bool touches_a0() {
-	return !(OP == Op1::Phase || OP == Op1::PhaseNeg || OP == Op1::PhaseI);
-}
 
 template <typename T, Op1 OP, int NINS>
 __global__ void __launch_bounds__(256) k_ctrl1q(cplx_t<T>* __restrict__ s, uint64_t items, Mat2<T> m, uint64_t tbit, BitPlan pl) {
@@ -201,6 +142,11 @@ cudaError_t launch_ctrl1q(cplx_t<T>* s, uint64_t N, Op1 op, const Mat2<T>& m, ui
 	case Op1::Real: return ctrl1q_nins<T, Op1::Real>(s, N, m, tbit, pl, sms, st);
 	case Op1::RxLike: return ctrl1q_nins<T, Op1::RxLike>(s, N, m, tbit, pl, sms, st);
 	case Op1::Generic: return ctrl1q_nins<T, Op1::Generic>(s, N, m, tbit, pl, sms, st);
+	case Op1::AntidiagUnit: return ctrl1q_nins<T, Op1::AntidiagUnit>(s, N, m, tbit, pl, sms, st);
+	case Op1::UnitRe01: return ctrl1q_nins<T, Op1::UnitRe01>(s, N, m, tbit, pl, sms, st);
+	case Op1::UnitRe10: return ctrl1q_nins<T, Op1::UnitRe10>(s, N, m, tbit, pl, sms, st);
+	case Op1::UnitIm01: return ctrl1q_nins<T, Op1::UnitIm01>(s, N, m, tbit, pl, sms, st);
+	case Op1::UnitIm10: return ctrl1q_nins<T, Op1::UnitIm10>(s, N, m, tbit, pl, sms, st);
 	}
 	return cudaErrorInvalidValue;
 }

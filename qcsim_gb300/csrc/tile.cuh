@@ -1,0 +1,46 @@
+// Shared-memory passes: one kernel applies a run of consecutive gates to the state with each CTA
+// holding a tile of 2^k amplitudes in shared memory (the k "tile qubits" vary inside a tile, the
+// other qubits are fixed per tile).  Low qubits 0..L-1 are always tile qubits, so every tile is read
+// and written as contiguous runs of 2^L amplitudes.
+#pragma once
+
+#include "engine.cuh"
+
+namespace qcs {
+
+enum class TKind : uint8_t { Ctrl1q = 0, Swap = 1, Dense2 = 2, Dense3 = 3, GlobalDiag = 4 };
+
+// one gate inside a pass, in tile-local bit positions
+struct TileOp {
+	uint8_t kind;      // TKind
+	uint8_t op;        // Op1 (Ctrl1q, GlobalDiag) or SwapKind (Swap)
+	uint8_t nins;      // number of local bit positions a work item does not enumerate
+	uint8_t pad;
+	uint32_t ins;      // those positions, ascending, 8 bits each (lowest byte first)
+	uint32_t lset;     // local control bits (forced to one in every work item)
+	uint32_t lbit0;    // Ctrl1q: target bit (0 = the factor sits on the target-bit-0 half); Swap: bit A; Dense: matrix bit 0
+	uint32_t lbit1;    // Swap: bit B; Dense: matrix bit 1
+	uint32_t lbit2;    // Dense3: matrix bit 2
+	uint32_t mat;      // offset of the op's entries in the pass matrix table (complex entries)
+	uint64_t gmask;    // non-tile controls: the op applies only in tiles whose fixed bits include these
+	uint64_t gtbit;    // GlobalDiag: the non-tile target bit selecting m00 (clear) or m11 (set)
+};
+
+// per-pass geometry
+struct TilePass {
+	int k;                 // tile qubits
+	int L;                 // qubits 0..L-1 are tile qubits
+	int nfixed;            // n - k
+	uint8_t high[32];      // global positions of local bits L..k-1
+	uint8_t fixed[40];     // global positions of the non-tile qubits, ascending
+	uint32_t op_begin, op_count;
+};
+
+template <typename T>
+cudaError_t launch_tile_pass(cplx_t<T>* s, const TilePass& p, const TileOp* d_ops, const cplx_t<T>* d_mats, int sms,
+                             cudaStream_t st);
+
+// largest tile (qubits) for the precision, given the shared memory per block
+template <typename T> int tile_qubits();
+
+}  // namespace qcs

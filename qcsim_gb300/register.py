@@ -81,6 +81,10 @@ class QubitRegister:
     def handle(self):
         return self._h
 
+    def set_passes(self, enabled: bool) -> None:
+        """gate lists as shared-memory passes (default) or one kernel per gate"""
+        self._ck(self._lib.qcs_set_option(self._h, L.QCS_OPT_PASSES, int(bool(enabled))))
+
     def seed(self, s: int) -> None:
         """reseed the register's generator (the reference's protected rng, QubitRegister.h:723)"""
         self.rng = Rng(s)

@@ -314,7 +314,57 @@ def test_fp32_register(Q):
     want = oracle_state(n, ops)
     got = reg.getRegisterStorage()
     assert np.abs(got - want).max() < 2e-6
+    # fidelity of the renormalised FP32 state (the FP32 path renormalises in FP64)
+    got = got / np.linalg.norm(got)
     assert 1 - abs(np.vdot(want, got)) ** 2 < 1e-9
+
+
+@pytest.mark.parametrize("n,precision", [(14, "fp64"), (16, "fp64"), (15, "fp32"), (17, "fp32")])
+def test_passes_match_per_gate(Q, n, precision):
+    """gate lists run as shared-memory passes give the per-gate results (every gate class, random
+    placements, matrix-only gates, long runs of diagonal gates on non-tile qubits)"""
+    from qcsim_gb300 import circuits, gates as G
+    r = np.random.default_rng(n)
+    codes = sorted(G.BY_CODE)
+    ops = []
+    for _ in range(300):
+        g = G.make(int(r.choice(codes)), *r.uniform(0, 2 * np.pi, 4))
+        qs = [int(x) for x in r.choice(n, size=3, replace=False)]
+        ops.append((g, *qs))
+    for k in (1, 2, 3):
+        a = r.standard_normal((1 << k, 1 << k)) + 1j * r.standard_normal((1 << k, 1 << k))
+        u, _ = np.linalg.qr(a)
+        qs = [int(x) for x in r.choice(n, size=3, replace=False)]
+        ops.append((G.AppliedGate(u, *qs), *qs))
+    ops += circuits.qft_circuit(0, n - 1)
+    init = rand_state(n, 4)
+    a = Q.QubitRegister(n, seed=1, precision=precision)
+    a.setRegisterStorageFastNoNormalize(init)
+    a.ApplyGates(ops)
+    b = Q.QubitRegister(n, seed=1, precision=precision)
+    b.set_passes(False)
+    b.setRegisterStorageFastNoNormalize(init)
+    b.ApplyGates(ops)
+    sa, sb = a.getRegisterStorage(), b.getRegisterStorage()
+    want = oracle_state(n, ops, init)
+    tol = TOL if precision == "fp64" else 5e-5
+    assert np.abs(sa - want).max() <= tol
+    assert np.abs(sb - want).max() <= tol
+    assert np.abs(sa - sb).max() <= (1e-14 if precision == "fp64" else 1e-6)
+
+
+def test_qft_passes(Q):
+    from qcsim_gb300 import algorithms, circuits
+    n = 20
+    v = circuits.random_normal_state(n, 11)
+    reg = Q.QubitRegister(n, seed=1)
+    reg.setRegisterStorageFastNoNormalize(v)
+    algorithms.QuantumFourierTransform(n).QFT(reg)
+    got = reg.getRegisterStorage()
+    # QFT|v> is the unitary DFT with e^{+2 pi i jk / N}: N * ifft(v) / sqrt(N) (the bit-reversing swaps included)
+    want = np.fft.ifft(v) * np.sqrt(v.size)
+    assert np.abs(got - want).max() <= TOL
+    assert np.abs(got - oracle_state(n, circuits.qft_circuit(0, n - 1), v)).max() <= TOL
 
 
 def test_larger_register_properties(Q):
