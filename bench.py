@@ -257,8 +257,11 @@ def run_gb300(args):
         step(i)
     torch.cuda.synchronize()
 
-    # timed region (device time, events on the engine's stream)
+    # timed region (device time, events on the engine's stream; the engine also brackets each of its
+    # launches with events so the dominant kernel's average duration comes from this same region)
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    reg.profile(True)
+    reg.read_profile()
     launches0 = lib.qcs_launch_count()
     with ClockSampler(local) as clk:
         barrier(dist)
@@ -274,11 +277,14 @@ def run_gb300(args):
         torch.cuda.synchronize()
         barrier(dist)
     launches = lib.qcs_launch_count() - launches0
+    prof = reg.read_profile()
+    reg.profile(False)
     ms = e0.elapsed_time(e1)
     ms_max = max_over_ranks(dist, ms)
     value = gates * world / (ms_max / 1e3)
     peak, peak_kind = peaks()
     hbm_frac = alg_bytes / (ms / 1e3) / (peak * 1e9)
+    roofline = roofline_of(prof, peak, peak_kind)
 
     # end to end through the C ABI: host gate records in, a qubit probability out, every step
     barrier(dist)
@@ -295,34 +301,32 @@ def run_gb300(args):
     e2e = {"value": gates * world / e2e_s, "unit": "gates/s", "h2d_bytes_per_step": h2d / args.steps,
            "d2h_bytes_per_step": 8}
 
-    # dominant kernel: every gate of one layer timed alone (same stream), grouped by kernel family
-    fam_time: dict[str, list] = {}
-    fam_bytes: dict[str, float] = {}
-    lay = layers[1]
-    for rep in range(3):
-        for op in lay:
-            rec = G.records([op])
-            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            a.record(stream)
-            reg.apply_records(rec)
-            b.record(stream)
-            b.synchronize()
-            fam = family(op[0])
-            fam_time.setdefault(fam, []).append(a.elapsed_time(b))
-            fam_bytes[fam] = algorithmic_bytes(op[0], n)
-    shares = {f: sum(v) for f, v in fam_time.items()}
-    dom = max(shares, key=shares.get)
-    dom_ms = statistics.mean(fam_time[dom])
-    achieved = fam_bytes[dom] / (dom_ms / 1e3) / 1e9
-    traffic = read_traffic(dom)
-    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                "traffic": traffic, "kernel": dom, "peak_source": peak_kind,
-                "algorithmic_bytes_per_launch": fam_bytes[dom], "avg_launch_ms": dom_ms,
-                "share_of_layer_time": shares[dom] / sum(shares.values())}
+    # the same layers with one kernel per gate (the plain per-gate path), profiled the same way
+    extra = {}
+    if rank == 0:
+        reg.set_passes(False)
+        reg.profile(True)
+        reg.read_profile()
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        pg_gates, pg_bytes = 0, 0.0
+        for i in range(min(args.steps, 6)):
+            step(i)
+            pg_gates += len(layers[i % len(layers)])
+            pg_bytes += bytes_layer[i % len(layers)]
+        b.record(stream)
+        b.synchronize()
+        pg_ms = a.elapsed_time(b)
+        pg_prof = reg.read_profile()
+        reg.profile(False)
+        reg.set_passes(True)
+        extra["per_gate"] = {"gates_per_s": pg_gates / (pg_ms / 1e3), "hbm_frac_per_gate": pg_bytes / (pg_ms / 1e3) / (peak * 1e9),
+                             "kernels": {k: {"launches": v[0], "ms": v[1], "GB/s": v[2] / (v[1] / 1e3) / 1e9 if v[1] else None}
+                                         for k, v in pg_prof.items()}}
 
     # QFT over all qubits, device-timed, one call (its time does not depend on the amplitudes, so the
     # circuit's output state serves as the input; QFT parity on random normal inputs is in the tests)
-    extra = {}
     if rank == 0:
         torch.cuda.synchronize()
         qops = circuits.qft_circuit(0, n - 1)
@@ -353,6 +357,19 @@ def run_gb300(args):
         print(json.dumps(line))
     if dist is not None:
         dist.destroy_process_group()
+
+
+def roofline_of(prof: dict, peak: float, peak_kind: str) -> dict:
+    """the kernel family with the largest share of device time: algorithmic bytes per launch over its
+    average launch duration"""
+    total = sum(v[1] for v in prof.values()) or 1.0
+    dom = max(prof, key=lambda k: prof[k][1])
+    launches, ms, nbytes = prof[dom]
+    achieved = nbytes / (ms / 1e3) / 1e9
+    return {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+            "traffic": read_traffic(dom), "kernel": dom, "peak_source": peak_kind,
+            "algorithmic_bytes_per_launch": nbytes / launches, "avg_launch_ms": ms / launches,
+            "share_of_device_time": ms / total, "launches": launches}
 
 
 def family(gate) -> str:

@@ -149,6 +149,20 @@ enum qcs_option {
 };
 int qcs_set_option(qcs_handle h, int option, int value);
 
+/* ---- launch timing (no reference counterpart: the reference has no profiler) ----
+ * When enabled, every kernel the register launches is bracketed by CUDA events on its stream.
+ * qcs_profile_read synchronises the stream, returns per kernel family the launch count, the summed
+ * device milliseconds and the summed algorithmic bytes (2 x amplitude bytes x amplitudes the launch
+ * must read and write), and clears the records. */
+typedef struct qcs_profile_entry {
+	char name[48];
+	uint64_t launches;
+	double milliseconds;
+	double bytes;
+} qcs_profile_entry;
+int qcs_profile_enable(qcs_handle h, int enable);
+int qcs_profile_read(qcs_handle h, qcs_profile_entry* out, int capacity, int* count_out);
+
 /* ---- engine statistics ---- */
 /* number of CUDA kernels this library has launched since it was loaded (all registers) */
 uint64_t qcs_launch_count(void);

@@ -94,11 +94,19 @@ SIGNATURES = {
     "qcs_restore_state_destructive": (_i, [_h]),
     "qcs_expectation": (_i, [_h, C.c_void_p, _sz, _pd]),
     "qcs_set_option": (_i, [_h, _i, _i]),
+    "qcs_profile_enable": (_i, [_h, _i]),
+    "qcs_profile_read": (_i, [_h, C.c_void_p, _i, C.POINTER(_i)]),
     "qcs_launch_count": (_u64, []),
     "qcs_rng_create": (_i, [_u64, C.POINTER(_h)]),
     "qcs_rng_destroy": (_i, [_h]),
     "qcs_rng_uniform": (_i, [_h, _pd, _sz]),
 }
+
+
+
+class qcs_profile_entry(C.Structure):
+    _fields_ = [("name", C.c_char * 48), ("launches", C.c_uint64), ("milliseconds", C.c_double), ("bytes", C.c_double)]
+
 
 _lib = None
 

@@ -77,8 +77,11 @@ int materialize(qcs_handle h) {
 // QubitRegister::ApplyGate (QubitRegister.h:434-486) through the compiled trait dispatch
 cudaError_t dispatch_one(qcs_handle h, const qcs_gate& g) {
 	const qcs::CompiledGate c = qcs::compile_gate(g, true);
+	if (c.kind != qcs::GKind::Identity)
+		qcs::prof_begin(h, qcs::kernel_name(c), 2.0 * h->amp_bytes() * static_cast<double>(h->N) * qcs::touched_fraction(c));
 	cudaError_t e = h->prec == QCS_FP64 ? qcs::launch_compiled<double>(static_cast<double2*>(h->d_state), h->N, c, h->sms, h->stream)
 	                                    : qcs::launch_compiled<float>(static_cast<float2*>(h->d_state), h->N, c, h->sms, h->stream);
+	qcs::prof_end(h);
 	if (e != cudaSuccess) return e;
 	h->scale *= c.scale;
 	const double mag = std::abs(h->scale);
@@ -182,6 +185,7 @@ void free_register(qcs_handle h) {
 	if (h->sc.d_out) cudaFree(h->sc.d_out);
 	if (h->sc.h_pinned) cudaFreeHost(h->sc.h_pinned);
 	qcs::batch_release(h);
+	qcs::prof_release(h);
 	if (h->own_stream && h->stream) cudaStreamDestroy(h->stream);
 	delete h;
 }

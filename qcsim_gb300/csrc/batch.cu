@@ -191,8 +191,11 @@ int run_planned(qcs_handle h, const std::vector<PlannedPass>& passes, int kmax, 
 		e = cudaMemcpyAsync(bb->d_mats, mats.data(), mats.size() * sizeof(cplx_t<T>), cudaMemcpyHostToDevice, h->stream);
 	auto* s = static_cast<cplx_t<T>*>(h->d_state);
 	for (size_t i = 0; i < tps.size() && e == cudaSuccess; ++i) {
-		if (tps[i].op_count > 0)
+		if (tps[i].op_count > 0) {
+			prof_begin(h, "tile_pass", 2.0 * sizeof(cplx_t<T>) * static_cast<double>(h->N));
 			e = launch_tile_pass<T>(s, tps[i], static_cast<const TileOp*>(bb->d_ops), static_cast<const cplx_t<T>*>(bb->d_mats), h->sms, h->stream);
+			prof_end(h);
+		}
 		const std::complex<double> f = passes[i].fold_after;
 		if (e == cudaSuccess && f != std::complex<double>(1.0, 0.0))
 			e = launch_scale_complex<T>(s, h->N, f.real(), f.imag(), h->sms, h->stream);

@@ -118,6 +118,30 @@ void add_ctrl(CompiledGate& c, uint32_t q) { c.controls[c.ncontrols++] = q; }
 
 }  // namespace
 
+const char* kernel_name(const CompiledGate& c) {
+	static const char* ops[] = {"ctrl1q_diag", "ctrl1q_phase", "ctrl1q_phaseneg", "ctrl1q_phasei", "ctrl1q_antidiag",
+	                            "ctrl1q_swap", "ctrl1q_real", "ctrl1q_rxlike", "ctrl1q_generic", "ctrl1q_antidiagunit",
+	                            "ctrl1q_unitre01", "ctrl1q_unitre10", "ctrl1q_unitim01", "ctrl1q_unitim10"};
+	switch (c.kind) {
+	case GKind::Ctrl1q: return ops[static_cast<int>(c.op)];
+	case GKind::Swap: return c.ncontrols ? "swap_controlled" : "swap";
+	case GKind::Dense: return c.dense_k == 2 ? "dense2" : "dense3";
+	default: return "identity";
+	}
+}
+
+double touched_fraction(const CompiledGate& c) {
+	const double ctl = 1.0 / static_cast<double>(1u << c.ncontrols);
+	switch (c.kind) {
+	case GKind::Ctrl1q:
+		if (c.op == Op1::Phase || c.op == Op1::PhaseNeg || c.op == Op1::PhaseI) return ctl * 0.5;
+		return ctl;
+	case GKind::Swap: return ctl * 0.5;
+	case GKind::Dense: return ctl;
+	default: return 0.0;
+	}
+}
+
 uint64_t CompiledGate::local_mask() const {
 	switch (kind) {
 	case GKind::Ctrl1q:

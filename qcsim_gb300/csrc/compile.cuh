@@ -38,6 +38,10 @@ struct CompiledGate {
 	uint64_t touch_mask() const;
 };
 
+// kernel family name (profiling) and the fraction of amplitudes the gate reads and writes
+const char* kernel_name(const CompiledGate& c);
+double touched_fraction(const CompiledGate& c);
+
 // `factor` allows taking a global scalar out of uncontrolled one-qubit gates
 CompiledGate compile_gate(const qcs_gate& g, bool factor);
 

@@ -91,12 +91,18 @@ struct qcs_register {
 	std::complex<double> scale{1.0, 0.0};  // amplitudes = scale * stored values
 	void* batch = nullptr;                 // planner buffers (batch.cu)
 	int batch_mode = 1;                    // QCS_OPT_PASSES
+	void* prof = nullptr;                  // launch timing records (profile.cu), when enabled
 	std::string err;
 	size_t amp_bytes() const { return prec == QCS_FP64 ? 16 : 8; }
 	size_t state_bytes() const { return static_cast<size_t>(N) * amp_bytes(); }
 };
 
 namespace qcs {
+
+// launch timing (profile.cu): no-ops unless profiling is enabled on the register
+void prof_begin(qcs_handle h, const char* name, double bytes);
+void prof_end(qcs_handle h);
+void prof_release(qcs_handle h);
 
 // ---- kernel launchers (gate_kernels.cu) ----
 template <typename T>

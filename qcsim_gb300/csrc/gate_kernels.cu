@@ -13,7 +13,7 @@
 namespace qcs {
 namespace {
 
-template <typename T, Op1 OP, int NINS>
+template <typename T, Op1 OP, int NINS, int SG>
 __global__ void __launch_bounds__(256) k_ctrl1q(cplx_t<T>* __restrict__ s, uint64_t items, Mat2<T> m, uint64_t tbit, BitPlan pl) {
 	const uint64_t stride = static_cast<uint64_t>(gridDim.x) * blockDim.x;
 	uint64_t p = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
@@ -23,8 +23,8 @@ __global__ void __launch_bounds__(256) k_ctrl1q(cplx_t<T>* __restrict__ s, uint6
 		if constexpr (touches_a0<OP>()) { x0 = s[b0]; y0 = s[b1]; }
 		x1 = s[b0 | tbit];
 		y1 = s[b1 | tbit];
-		op2<T, OP>(x0, x1, m);
-		op2<T, OP>(y0, y1, m);
+		op2<T, OP, SG>(x0, x1, m);
+		op2<T, OP, SG>(y0, y1, m);
 		if constexpr (touches_a0<OP>()) { s[b0] = x0; s[b1] = y0; }
 		s[b0 | tbit] = x1;
 		s[b1 | tbit] = y1;
@@ -34,7 +34,7 @@ __global__ void __launch_bounds__(256) k_ctrl1q(cplx_t<T>* __restrict__ s, uint6
 		cplx_t<T> x0, x1;
 		if constexpr (touches_a0<OP>()) x0 = s[b0];
 		x1 = s[b0 | tbit];
-		op2<T, OP>(x0, x1, m);
+		op2<T, OP, SG>(x0, x1, m);
 		if constexpr (touches_a0<OP>()) s[b0] = x0;
 		s[b0 | tbit] = x1;
 	}
@@ -99,18 +99,34 @@ __global__ void __launch_bounds__(256) k_dense(cplx_t<T>* __restrict__ s, uint64
 	}
 }
 
-template <typename T, Op1 OP>
-cudaError_t ctrl1q_nins(cplx_t<T>* s, uint64_t N, const Mat2<T>& m, uint64_t tbit, const BitPlan& pl, int sms, cudaStream_t st) {
+template <typename T, Op1 OP, int SG>
+cudaError_t ctrl1q_sg(cplx_t<T>* s, uint64_t N, const Mat2<T>& m, uint64_t tbit, const BitPlan& pl, int sms, cudaStream_t st) {
 	const uint64_t items = N >> pl.nins;
 	const int grid = grid_for((items + 1) / 2, 256, sms);
 	switch (pl.nins) {
-	case 1: k_ctrl1q<T, OP, 1><<<grid, 256, 0, st>>>(s, items, m, tbit, pl); break;
-	case 2: k_ctrl1q<T, OP, 2><<<grid, 256, 0, st>>>(s, items, m, tbit, pl); break;
-	case 3: k_ctrl1q<T, OP, 3><<<grid, 256, 0, st>>>(s, items, m, tbit, pl); break;
+	case 1: k_ctrl1q<T, OP, 1, SG><<<grid, 256, 0, st>>>(s, items, m, tbit, pl); break;
+	case 2: k_ctrl1q<T, OP, 2, SG><<<grid, 256, 0, st>>>(s, items, m, tbit, pl); break;
+	case 3: k_ctrl1q<T, OP, 3, SG><<<grid, 256, 0, st>>>(s, items, m, tbit, pl); break;
 	default: return cudaErrorInvalidValue;
 	}
 	note_launches(1);
 	return cudaGetLastError();
+}
+
+// the Unit* forms carry the signs of their unit entries in m00.x / m01.x; they select the kernel
+template <typename T, Op1 OP>
+cudaError_t ctrl1q_nins(cplx_t<T>* s, uint64_t N, const Mat2<T>& m, uint64_t tbit, const BitPlan& pl, int sms, cudaStream_t st) {
+	if constexpr (OP == Op1::UnitRe01 || OP == Op1::UnitRe10 || OP == Op1::UnitIm01 || OP == Op1::UnitIm10) {
+		const int sgn = (m.m00.x < 0 ? 1 : 0) | (m.m01.x < 0 ? 2 : 0);
+		switch (sgn) {
+		case 0: return ctrl1q_sg<T, OP, 0>(s, N, m, tbit, pl, sms, st);
+		case 1: return ctrl1q_sg<T, OP, 1>(s, N, m, tbit, pl, sms, st);
+		case 2: return ctrl1q_sg<T, OP, 2>(s, N, m, tbit, pl, sms, st);
+		default: return ctrl1q_sg<T, OP, 3>(s, N, m, tbit, pl, sms, st);
+		}
+	} else {
+		return ctrl1q_sg<T, OP, 0>(s, N, m, tbit, pl, sms, st);
+	}
 }
 
 template <typename T, SwapKind K>

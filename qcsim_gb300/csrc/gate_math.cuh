@@ -32,14 +32,16 @@ template <typename T> __device__ __forceinline__ cplx_t<T> mul_unit(const cplx_t
 	}
 }
 
-template <typename T> __device__ __forceinline__ T sgn_sel(T s, T v) { return s < 0 ? -v : v; }
+// v or -v, chosen at compile time (the negation folds into the consuming FMA)
+template <int NEG, typename T> __device__ __forceinline__ T sg(T v) { return NEG ? -v : v; }
 
 // 2x2 block update of (a0, a1) = (amplitude with target bit 0, with target bit 1).
 // Mat2 field use per op:
 //   Diag/Phase*: m00, m11 diagonal entries        Antidiag: m01, m10
 //   AntidiagUnit: m01.x, m10.x hold unit codes    Real/RxLike/Generic: the four entries
 //   Unit*: m00 = (sigma0, x0), m01 = (sigma1, x1) -- see below
-template <typename T, Op1 OP>
+// SG: signs of the unit entries of the Unit* forms (bit 0: row 0 negative, bit 1: row 1 negative)
+template <typename T, Op1 OP, int SG = 0>
 __device__ __forceinline__ void op2(cplx_t<T>& a0, cplx_t<T>& a1, const Mat2<T>& m) {
 	if constexpr (OP == Op1::Diag) {
 		a0 = cmul<T>(a0, m.m00);
@@ -74,27 +76,27 @@ __device__ __forceinline__ void op2(cplx_t<T>& a0, cplx_t<T>& a1, const Mat2<T>&
 		a0 = n0;
 	} else if constexpr (OP == Op1::UnitRe01) {
 		// out0 = s0*a0 + x0*a1, out1 = s1*a1 + x1*a0 (s = +-1, x real)
-		const T s0 = m.m00.x, x0 = m.m00.y, s1 = m.m01.x, x1 = m.m01.y;
-		const cplx_t<T> n0 = mk<T>(fma(x0, a1.x, sgn_sel(s0, a0.x)), fma(x0, a1.y, sgn_sel(s0, a0.y)));
-		a1 = mk<T>(fma(x1, a0.x, sgn_sel(s1, a1.x)), fma(x1, a0.y, sgn_sel(s1, a1.y)));
+		const T x0 = m.m00.y, x1 = m.m01.y;
+		const cplx_t<T> n0 = mk<T>(fma(x0, a1.x, sg<SG & 1>(a0.x)), fma(x0, a1.y, sg<SG & 1>(a0.y)));
+		a1 = mk<T>(fma(x1, a0.x, sg<(SG >> 1) & 1>(a1.x)), fma(x1, a0.y, sg<(SG >> 1) & 1>(a1.y)));
 		a0 = n0;
 	} else if constexpr (OP == Op1::UnitRe10) {
 		// out0 = s0*a1 + x0*a0, out1 = s1*a0 + x1*a1
-		const T s0 = m.m00.x, x0 = m.m00.y, s1 = m.m01.x, x1 = m.m01.y;
-		const cplx_t<T> n0 = mk<T>(fma(x0, a0.x, sgn_sel(s0, a1.x)), fma(x0, a0.y, sgn_sel(s0, a1.y)));
-		a1 = mk<T>(fma(x1, a1.x, sgn_sel(s1, a0.x)), fma(x1, a1.y, sgn_sel(s1, a0.y)));
+		const T x0 = m.m00.y, x1 = m.m01.y;
+		const cplx_t<T> n0 = mk<T>(fma(x0, a0.x, sg<SG & 1>(a1.x)), fma(x0, a0.y, sg<SG & 1>(a1.y)));
+		a1 = mk<T>(fma(x1, a1.x, sg<(SG >> 1) & 1>(a0.x)), fma(x1, a1.y, sg<(SG >> 1) & 1>(a0.y)));
 		a0 = n0;
 	} else if constexpr (OP == Op1::UnitIm01) {
 		// out0 = s0*a0 + i*x0*a1, out1 = s1*a1 + i*x1*a0
-		const T s0 = m.m00.x, x0 = m.m00.y, s1 = m.m01.x, x1 = m.m01.y;
-		const cplx_t<T> n0 = mk<T>(fma(-x0, a1.y, sgn_sel(s0, a0.x)), fma(x0, a1.x, sgn_sel(s0, a0.y)));
-		a1 = mk<T>(fma(-x1, a0.y, sgn_sel(s1, a1.x)), fma(x1, a0.x, sgn_sel(s1, a1.y)));
+		const T x0 = m.m00.y, x1 = m.m01.y;
+		const cplx_t<T> n0 = mk<T>(fma(-x0, a1.y, sg<SG & 1>(a0.x)), fma(x0, a1.x, sg<SG & 1>(a0.y)));
+		a1 = mk<T>(fma(-x1, a0.y, sg<(SG >> 1) & 1>(a1.x)), fma(x1, a0.x, sg<(SG >> 1) & 1>(a1.y)));
 		a0 = n0;
 	} else if constexpr (OP == Op1::UnitIm10) {
 		// out0 = s0*a1 + i*x0*a0, out1 = s1*a0 + i*x1*a1
-		const T s0 = m.m00.x, x0 = m.m00.y, s1 = m.m01.x, x1 = m.m01.y;
-		const cplx_t<T> n0 = mk<T>(fma(-x0, a0.y, sgn_sel(s0, a1.x)), fma(x0, a0.x, sgn_sel(s0, a1.y)));
-		a1 = mk<T>(fma(-x1, a1.y, sgn_sel(s1, a0.x)), fma(x1, a1.x, sgn_sel(s1, a0.y)));
+		const T x0 = m.m00.y, x1 = m.m01.y;
+		const cplx_t<T> n0 = mk<T>(fma(-x0, a0.y, sg<SG & 1>(a1.x)), fma(x0, a0.x, sg<SG & 1>(a1.y)));
+		a1 = mk<T>(fma(-x1, a1.y, sg<(SG >> 1) & 1>(a0.x)), fma(x1, a1.x, sg<(SG >> 1) & 1>(a0.y)));
 		a0 = n0;
 	} else {
 		const cplx_t<T> n0 = mk<T>(m.m00.x * a0.x - m.m00.y * a0.y + m.m01.x * a1.x - m.m01.y * a1.y,

@@ -10,10 +10,15 @@ namespace {
 constexpr int kTileThreads = 512;
 constexpr int kMaxHigh = 8;  // at most 8 tile qubits above the contiguous low block
 
-__device__ __forceinline__ uint32_t expand_local(uint32_t i, const TileOp& op) {
+// the loop-invariant fields of a TileOp, held in registers
+struct OpRegs {
+	uint32_t ins, nins, lset, lbit0, lbit1, lbit2, mat;
+};
+
+__device__ __forceinline__ uint32_t expand_local(uint32_t i, const OpRegs& op) {
 	uint32_t packed = op.ins;
-	for (int j = 0; j < op.nins; ++j) {
-		const int b = static_cast<int>(packed & 0xffu);
+	for (uint32_t j = 0; j < op.nins; ++j) {
+		const uint32_t b = packed & 0xffu;
 		packed >>= 8;
 		i = ((i >> b) << (b + 1)) | (i & ((1u << b) - 1));
 	}
@@ -29,22 +34,33 @@ template <typename T> __device__ __forceinline__ Mat2<T> load_mat2(const cplx_t<
 	return m;
 }
 
-template <typename T, Op1 OP>
-__device__ __forceinline__ void tile_ctrl1q(cplx_t<T>* sm, uint32_t items, const TileOp& op, const Mat2<T>& m) {
+template <typename T, Op1 OP, int SG = 0>
+__device__ __forceinline__ void tile_ctrl1q(cplx_t<T>* sm, uint32_t items, const OpRegs op, const Mat2<T> m) {
 	for (uint32_t i = threadIdx.x; i < items; i += blockDim.x) {
 		const uint32_t b = expand_local(i, op);
 		cplx_t<T> a0, a1;
 		if constexpr (touches_a0<OP>()) a0 = sm[b];
 		a1 = sm[b | op.lbit0];
-		op2<T, OP>(a0, a1, m);
+		op2<T, OP, SG>(a0, a1, m);
 		if constexpr (touches_a0<OP>()) sm[b] = a0;
 		sm[b | op.lbit0] = a1;
 	}
 }
 
+template <typename T, Op1 OP>
+__device__ __forceinline__ void tile_unit(cplx_t<T>* sm, uint32_t items, const OpRegs op, const Mat2<T> m) {
+	const int sgn = (m.m00.x < 0 ? 1 : 0) | (m.m01.x < 0 ? 2 : 0);
+	switch (sgn) {
+	case 0: tile_ctrl1q<T, OP, 0>(sm, items, op, m); break;
+	case 1: tile_ctrl1q<T, OP, 1>(sm, items, op, m); break;
+	case 2: tile_ctrl1q<T, OP, 2>(sm, items, op, m); break;
+	default: tile_ctrl1q<T, OP, 3>(sm, items, op, m); break;
+	}
+}
+
 // diagonal whose target is not a tile qubit: one factor for the whole tile (restricted to local controls)
 template <typename T, Op1 OP>
-__device__ __forceinline__ void tile_globaldiag(cplx_t<T>* sm, uint32_t items, const TileOp& op, const Mat2<T>& m, bool bit_set) {
+__device__ __forceinline__ void tile_globaldiag(cplx_t<T>* sm, uint32_t items, const OpRegs op, const Mat2<T> m, bool bit_set) {
 	Mat2<T> mm = m;
 	if constexpr (OP == Op1::Diag) {
 		mm.m11 = bit_set ? m.m11 : m.m00;
@@ -64,22 +80,22 @@ __device__ __forceinline__ void tile_globaldiag(cplx_t<T>* sm, uint32_t items, c
 }
 
 template <typename T, int K>
-__device__ __noinline__ void tile_dense(cplx_t<T>* sm, uint32_t items, const TileOp& op, const cplx_t<T>* __restrict__ mats) {
+__device__ __forceinline__ void tile_dense(cplx_t<T>* sm, uint32_t items, const OpRegs op, const cplx_t<T>* __restrict__ mats) {
 	constexpr int D = 1 << K;
 	for (uint32_t i = threadIdx.x; i < items; i += blockDim.x) {
 		const uint32_t b = expand_local(i, op);
-		uint32_t idx[D];
+		// all inputs in registers first; each output row then goes straight to shared memory (no other
+		// thread touches this group)
 		cplx_t<T> v[D];
 #pragma unroll
-		for (int r = 0; r < D; ++r) {
+		for (int c = 0; c < D; ++c) {
 			uint32_t x = b;
-			if (r & 1) x |= op.lbit0;
-			if (K > 1 && (r & 2)) x |= op.lbit1;
-			if (K > 2 && (r & 4)) x |= op.lbit2;
-			idx[r] = x;
-			v[r] = sm[x];
+			if (c & 1) x |= op.lbit0;
+			if (K > 1 && (c & 2)) x |= op.lbit1;
+			if (K > 2 && (c & 4)) x |= op.lbit2;
+			v[c] = sm[x];
 		}
-#pragma unroll
+#pragma unroll 1
 		for (int r = 0; r < D; ++r) {
 			T re = 0, im = 0;
 #pragma unroll
@@ -88,18 +104,23 @@ __device__ __noinline__ void tile_dense(cplx_t<T>* sm, uint32_t items, const Til
 				re += mm.x * v[c].x - mm.y * v[c].y;
 				im += mm.x * v[c].y + mm.y * v[c].x;
 			}
-			sm[idx[r]] = mk<T>(re, im);
+			uint32_t x = b;
+			if (r & 1) x |= op.lbit0;
+			if (K > 1 && (r & 2)) x |= op.lbit1;
+			if (K > 2 && (r & 4)) x |= op.lbit2;
+			sm[x] = mk<T>(re, im);
 		}
 	}
 }
 
 template <typename T>
-__device__ void tile_apply(cplx_t<T>* sm, int k, const TileOp& op, const cplx_t<T>* __restrict__ mats, uint64_t base) {
+__device__ __forceinline__ void tile_apply(cplx_t<T>* sm, int k, const TileOp& top, const cplx_t<T>* __restrict__ mats, uint64_t base) {
+	const OpRegs op{top.ins, top.nins, top.lset, top.lbit0, top.lbit1, top.lbit2, top.mat};
 	const uint32_t items = (1u << k) >> op.nins;
-	const TKind kind = static_cast<TKind>(op.kind);
+	const TKind kind = static_cast<TKind>(top.kind);
 	if (kind == TKind::Ctrl1q) {
 		const Mat2<T> m = load_mat2<T>(mats, op.mat);
-		switch (static_cast<Op1>(op.op)) {
+		switch (static_cast<Op1>(top.op)) {
 		case Op1::Diag: tile_ctrl1q<T, Op1::Diag>(sm, items, op, m); break;
 		case Op1::Phase: tile_ctrl1q<T, Op1::Phase>(sm, items, op, m); break;
 		case Op1::PhaseNeg: tile_ctrl1q<T, Op1::PhaseNeg>(sm, items, op, m); break;
@@ -110,15 +131,15 @@ __device__ void tile_apply(cplx_t<T>* sm, int k, const TileOp& op, const cplx_t<
 		case Op1::Real: tile_ctrl1q<T, Op1::Real>(sm, items, op, m); break;
 		case Op1::RxLike: tile_ctrl1q<T, Op1::RxLike>(sm, items, op, m); break;
 		case Op1::Generic: tile_ctrl1q<T, Op1::Generic>(sm, items, op, m); break;
-		case Op1::UnitRe01: tile_ctrl1q<T, Op1::UnitRe01>(sm, items, op, m); break;
-		case Op1::UnitRe10: tile_ctrl1q<T, Op1::UnitRe10>(sm, items, op, m); break;
-		case Op1::UnitIm01: tile_ctrl1q<T, Op1::UnitIm01>(sm, items, op, m); break;
-		case Op1::UnitIm10: tile_ctrl1q<T, Op1::UnitIm10>(sm, items, op, m); break;
+		case Op1::UnitRe01: tile_unit<T, Op1::UnitRe01>(sm, items, op, m); break;
+		case Op1::UnitRe10: tile_unit<T, Op1::UnitRe10>(sm, items, op, m); break;
+		case Op1::UnitIm01: tile_unit<T, Op1::UnitIm01>(sm, items, op, m); break;
+		case Op1::UnitIm10: tile_unit<T, Op1::UnitIm10>(sm, items, op, m); break;
 		}
 	} else if (kind == TKind::GlobalDiag) {
 		const Mat2<T> m = load_mat2<T>(mats, op.mat);
-		const bool bit = (base & op.gtbit) != 0;
-		switch (static_cast<Op1>(op.op)) {
+		const bool bit = (base & top.gtbit) != 0;
+		switch (static_cast<Op1>(top.op)) {
 		case Op1::Diag: tile_globaldiag<T, Op1::Diag>(sm, items, op, m, bit); break;
 		case Op1::Phase: tile_globaldiag<T, Op1::Phase>(sm, items, op, m, bit); break;
 		case Op1::PhaseNeg: tile_globaldiag<T, Op1::PhaseNeg>(sm, items, op, m, bit); break;
@@ -126,7 +147,7 @@ __device__ void tile_apply(cplx_t<T>* sm, int k, const TileOp& op, const cplx_t<
 		default: break;
 		}
 	} else if (kind == TKind::Swap) {
-		const SwapKind sk = static_cast<SwapKind>(op.op);
+		const SwapKind sk = static_cast<SwapKind>(top.op);
 		for (uint32_t i = threadIdx.x; i < items; i += blockDim.x) {
 			const uint32_t b = expand_local(i, op);
 			const cplx_t<T> a = sm[b | op.lbit0], c = sm[b | op.lbit1];

@@ -85,6 +85,19 @@ class QubitRegister:
         """gate lists as shared-memory passes (default) or one kernel per gate"""
         self._ck(self._lib.qcs_set_option(self._h, L.QCS_OPT_PASSES, int(bool(enabled))))
 
+    def profile(self, enable: bool = True) -> None:
+        """bracket every kernel launch of this register with CUDA events (see read_profile)"""
+        self._ck(self._lib.qcs_profile_enable(self._h, int(bool(enable))))
+
+    def read_profile(self) -> dict:
+        """{kernel family: (launches, device ms, algorithmic bytes)} since the last read"""
+        cap = 64
+        arr = (L.qcs_profile_entry * cap)()
+        n = C.c_int()
+        self._ck(self._lib.qcs_profile_read(self._h, C.cast(arr, C.c_void_p), cap, C.byref(n)))
+        return {arr[i].name.decode(): (int(arr[i].launches), float(arr[i].milliseconds), float(arr[i].bytes))
+                for i in range(n.value)}
+
     def seed(self, s: int) -> None:
         """reseed the register's generator (the reference's protected rng, QubitRegister.h:723)"""
         self.rng = Rng(s)

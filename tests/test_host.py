@@ -105,3 +105,31 @@ def test_engine_rng_matches_reference(golden):
     from qcsim_gb300.register import Rng
     for row, seed in zip(golden["rng_uniforms"], (1, 7, 123456789)):
         assert np.array_equal(Rng(seed).uniform(row.size), row)
+
+
+REF_QCSIM = Path("/root/reference/QCSim")
+
+
+@pytest.mark.skipif(not REF_QCSIM.exists(), reason="needs the QCSim sources")
+def test_cpp_dropin_compiles_against_reference_headers():
+    """QCSim's own algorithm headers (QFT, Grover, Draper adder, QAOA, phase estimation), unmodified,
+    compile and link against the GPU-backed QubitRegister.h of qcsim_gb300/cpp.  The reference's
+    quoted includes are resolved through the include path (-I-), so the drop-in headers win."""
+    import glob
+    import shutil
+    import subprocess
+    if not L.LIB_PATH.exists():
+        pytest.skip("libqcs_gpu.so not built")
+    gxx = shutil.which("g++")
+    if not gxx:
+        pytest.skip("no g++")
+    pstl = sorted(glob.glob("/usr/include/c++/*/pstl"))
+    out = ROOT / "qcsim_gb300" / "_build"
+    out.mkdir(exist_ok=True)
+    cmd = [gxx, "-std=c++17", "-O1", f"-I{ROOT / 'qcsim_gb300' / 'cpp'}", f"-I{ROOT / 'include'}", f"-I{REF_QCSIM}", "-I-",
+           f"-I{ROOT / 'oracle' / 'eigen_shim'}"] + [f"-I{p}" for p in pstl[-1:]] + [
+           str(ROOT / "tests" / "cpp" / "dropin_check.cpp"), "-o", str(out / "dropin_check"),
+           f"-L{L.LIB_PATH.parent}", "-lqcs_gpu", f"-Wl,-rpath,{L.LIB_PATH.parent}"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr[-3000:]
+    assert (out / "dropin_check").exists()
