@@ -43,6 +43,9 @@ def parse():
     ap.add_argument("--seed", type=int, default=1)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-gates", type=int, default=6, help="gates per CPU step / sample")
+    ap.add_argument("--config", default="layered", choices=["layered", "precision"],
+                    help="layered: the 30-qubit FP64 circuit (headline); precision: fused FP32 vs plain FP64")
+    ap.add_argument("--max-block", type=int, default=5, help="precision config: largest fused block")
     return ap.parse_args()
 
 
@@ -392,8 +395,53 @@ def read_traffic(kernel_family: str):
     return None
 
 
+def run_precision(args):
+    """fused FP32 (dense blocks of <= max_block qubits) against plain FP64 on the same layered circuit:
+    device time of each and the fidelity / max amplitude error of the FP32 result"""
+    import ctypes as C
+    import torch
+    import qcsim_gb300 as Q
+    from qcsim_gb300 import _lib as L, circuits, gates as G
+    lib = L.load()
+    n = args.qubits
+    ops = circuits.layered_circuit(n, args.depth, seed=args.seed)
+    recs = G.records(ops)
+    stream = torch.cuda.Stream()
+    out = {}
+    regs = {}
+    for prec in ("fp64", "fp32"):
+        reg = Q.QubitRegister(n, seed=args.seed, precision=prec)
+        lib.qcs_set_stream(reg.handle, stream.cuda_stream)
+        if prec == "fp32":
+            reg.set_fusion(1, args.max_block)
+        reg.profile(True)
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        reg.apply_records(recs)
+        b.record(stream)
+        b.synchronize()
+        prof = reg.read_profile()
+        reg.profile(False)
+        out[prec] = {"seconds": a.elapsed_time(b) / 1e3, "kernels": {k: {"launches": v[0], "ms": v[1]} for k, v in prof.items()}}
+        regs[prec] = reg
+    f, d = C.c_double(), C.c_double()
+    L.check(lib.qcs_compare(regs["fp64"].handle, regs["fp32"].handle, C.byref(f), C.byref(d)), regs["fp64"].handle)
+    line = {"metric": "fused FP32 vs plain FP64 time @1-F<=1e-6", "config": {
+                "workload": f"layered random circuit, {n} qubits, depth {args.depth}, seed {args.seed}",
+                "gates": len(ops), "max_block_qubits": args.max_block},
+            "fp64_seconds": out["fp64"]["seconds"], "fp32_fused_seconds": out["fp32"]["seconds"],
+            "speedup": out["fp64"]["seconds"] / out["fp32"]["seconds"], "one_minus_fidelity": 1.0 - f.value,
+            "max_abs_amplitude_error": d.value, "fp64_kernels": out["fp64"]["kernels"],
+            "fp32_kernels": out["fp32"]["kernels"], "data": "synthetic"}
+    print(json.dumps(line))
+
+
 def main():
     args = parse()
+    if args.config == "precision":
+        run_precision(args)
+        return
     if args.impl == "reference":
         run_reference(args)
     else:

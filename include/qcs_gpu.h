@@ -136,6 +136,11 @@ int qcs_fidelity_host(qcs_handle h, const double* host_state, double* f_out);
 /* <h|other> between two registers of the same size (the product inside stateFidelity / ExpectationValue) */
 int qcs_inner(qcs_handle h, qcs_handle other, double* re_im_out);
 
+/* two registers of the same size and any precisions: the normalised fidelity
+ * |<h|other>|^2 / (|h|^2 |other|^2) and the largest |h_i - other_i|.  No reference counterpart: it
+ * reports the FP32 path's accuracy against an FP64 run of the same circuit. */
+int qcs_compare(qcs_handle h, qcs_handle other, double* fidelity_out, double* max_abs_diff_out);
+
 /* ---- snapshots (SaveState / RestoreState / RestoreStateDestructive, QubitRegister.h:600-616) ---- */
 int qcs_save_state(qcs_handle h);
 int qcs_restore_state(qcs_handle h);                 /* no-op when nothing was saved */
@@ -145,7 +150,10 @@ int qcs_expectation(qcs_handle h, const qcs_gate* gates, size_t count, double* r
 
 /* ---- engine options ---- */
 enum qcs_option {
-	QCS_OPT_PASSES = 1 /* 1 (default): gate lists run as shared-memory passes; 0: one kernel per gate */
+	QCS_OPT_PASSES = 1,          /* 1 (default): gate lists run as shared-memory passes; 0: one kernel per gate */
+	QCS_OPT_FUSION = 2,          /* gate lists fused into dense blocks: 0 off (FP64 default), 1 greedy (FP32
+	                                default), 2 partition chosen by the learned cost model when one is loaded */
+	QCS_OPT_FUSION_MAX_QUBITS = 3 /* largest fused block (1..5; FP64 registers use at most 4) */
 };
 int qcs_set_option(qcs_handle h, int option, int value);
 

@@ -18,6 +18,8 @@ LIB_PATH = Path(os.environ.get("QCS_GPU_LIB", PKG / "libqcs_gpu.so"))
 QCS_OK, QCS_INVALID_ARGUMENT, QCS_OUT_OF_MEMORY, QCS_CUDA_ERROR, QCS_UNSUPPORTED = range(5)
 QCS_FP64, QCS_FP32 = 0, 1
 QCS_OPT_PASSES = 1
+QCS_OPT_FUSION = 2
+QCS_OPT_FUSION_MAX_QUBITS = 3
 
 TRAIT_DIAGONAL = 1
 TRAIT_ANTIDIAGONAL = 2
@@ -89,6 +91,7 @@ SIGNATURES = {
     "qcs_probabilities": (_i, [_h, _pd]),
     "qcs_fidelity_host": (_i, [_h, _pd, _pd]),
     "qcs_inner": (_i, [_h, _h, _pd]),
+    "qcs_compare": (_i, [_h, _h, _pd, _pd]),
     "qcs_save_state": (_i, [_h]),
     "qcs_restore_state": (_i, [_h]),
     "qcs_restore_state_destructive": (_i, [_h]),

@@ -293,6 +293,16 @@ int qcs_set_option(qcs_handle h, int option, int value) {
 		h->batch_mode = value ? 1 : 0;
 		return QCS_OK;
 	}
+	if (option == QCS_OPT_FUSION) {
+		if (value < 0 || value > 2) return fail(h, QCS_INVALID_ARGUMENT, "fusion mode must be 0, 1 or 2");
+		h->fusion = value;
+		return QCS_OK;
+	}
+	if (option == QCS_OPT_FUSION_MAX_QUBITS) {
+		if (value < 1 || value > 5) return fail(h, QCS_INVALID_ARGUMENT, "fused blocks hold 1 to 5 qubits");
+		h->fusion_max = value;
+		return QCS_OK;
+	}
 	return fail(h, QCS_INVALID_ARGUMENT, "unknown option");
 }
 

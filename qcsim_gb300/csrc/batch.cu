@@ -12,6 +12,7 @@
 
 #include "batch.cuh"
 #include "compile.cuh"
+#include "fusion.cuh"
 #include "tile.cuh"
 
 namespace qcs {
@@ -167,6 +168,15 @@ int run_planned(qcs_handle h, const std::vector<PlannedPass>& passes, int kmax, 
 					v.y = static_cast<T>(c.dense_m[2 * i + 1]);
 					mats.push_back(v);
 				}
+			} else if (c.kind == GKind::Block) {
+				op.kind = static_cast<uint8_t>(TKind::DenseN);
+				for (uint32_t q : c.block_q) ins.push_back(lpos[q]);
+				for (const std::complex<double>& x : c.block_m) {
+					cplx_t<T> v;
+					v.x = static_cast<T>(x.real());
+					v.y = static_cast<T>(x.imag());
+					mats.push_back(v);
+				}
 			} else {
 				continue;
 			}
@@ -211,8 +221,52 @@ int run_planned(qcs_handle h, const std::vector<PlannedPass>& passes, int kmax, 
 
 }  // namespace
 
+// the fused path: blocks of up to fusion_max qubits, each one dense matrix, applied in shared-memory passes
+int fused_apply(qcs_handle h, const qcs_gate* gates, size_t count) {
+	const int n = static_cast<int>(h->n);
+	std::vector<CompiledGate> cg;
+	cg.reserve(count);
+	for (size_t i = 0; i < count; ++i) cg.push_back(compile_gate(gates[i], false));
+	FusionPolicy pol;
+	pol.max_qubits = std::min(h->fusion_max, h->prec == QCS_FP64 ? 4 : 5);
+	pol.nqubits = n;
+	if (h->fusion == 2 && h->cost_model) {
+		pol.cost = h->cost_model;
+		pol.ctx = h->cost_ctx;
+	}
+	std::vector<FusedBlock> blocks = fuse(cg, pol);
+	const int kfull = h->prec == QCS_FP64 ? tile_qubits<double>() : tile_qubits<float>();
+	const int kmax = std::min(kfull, n);
+	const int L0 = std::min(n, std::max(5, kmax - 8));
+	std::vector<PlannedPass> passes(1);
+	passes.back().tmask = (1ULL << L0) - 1;
+	for (FusedBlock& b : blocks) {
+		if (b.qubits.empty()) {  // a global factor only
+			h->scale *= b.M[0];
+			continue;
+		}
+		CompiledGate c;
+		c.kind = GKind::Block;
+		c.block_q = b.qubits;
+		c.block_m = std::move(b.M);
+		c.block_gates = b.ngates;
+		const uint64_t need = c.local_mask();
+		if (popcount64(passes.back().tmask | need) > kmax) {
+			passes.emplace_back();
+			passes.back().tmask = ((1ULL << L0) - 1) | need;
+		} else {
+			passes.back().tmask |= need;
+		}
+		passes.back().gates.push_back(std::move(c));
+	}
+	h->last_blocks = blocks.size();
+	return h->prec == QCS_FP64 ? run_planned<double>(h, passes, kmax, L0) : run_planned<float>(h, passes, kmax, L0);
+}
+
 int batch_apply(qcs_handle h, const qcs_gate* gates, size_t count) {
 	const int n = static_cast<int>(h->n);
+	const int fusion = h->fusion >= 0 ? h->fusion : (h->prec == QCS_FP32 ? 1 : 0);
+	if (fusion > 0 && count > 0) return fused_apply(h, gates, count);
 	const int kmax = h->prec == QCS_FP64 ? tile_qubits<double>() : tile_qubits<float>();
 	if (n < kmax + 2 || count < 2 || h->batch_mode == 0) {
 		for (size_t i = 0; i < count; ++i) {

@@ -126,6 +126,7 @@ const char* kernel_name(const CompiledGate& c) {
 	case GKind::Ctrl1q: return ops[static_cast<int>(c.op)];
 	case GKind::Swap: return c.ncontrols ? "swap_controlled" : "swap";
 	case GKind::Dense: return c.dense_k == 2 ? "dense2" : "dense3";
+	case GKind::Block: return "block";
 	default: return "identity";
 	}
 }
@@ -138,6 +139,7 @@ double touched_fraction(const CompiledGate& c) {
 		return ctl;
 	case GKind::Swap: return ctl * 0.5;
 	case GKind::Dense: return ctl;
+	case GKind::Block: return 1.0;
 	default: return 0.0;
 	}
 }
@@ -151,6 +153,11 @@ uint64_t CompiledGate::local_mask() const {
 	case GKind::Dense: {
 		uint64_t m = 0;
 		for (int j = 0; j < dense_k; ++j) m |= 1ULL << dense_q[j];
+		return m;
+	}
+	case GKind::Block: {
+		uint64_t m = 0;
+		for (uint32_t q : block_q) m |= 1ULL << q;
 		return m;
 	}
 	default: return 0;

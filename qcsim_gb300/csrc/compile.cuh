@@ -14,7 +14,8 @@ enum class GKind : int {
 	Identity = 0,  // nothing to do (e.g. a diagonal gate whose read entries are both 1)
 	Ctrl1q,        // 2x2 block on `target`, under `controls`
 	Swap,          // exchange base|bitA with base|bitB, under `controls`
-	Dense          // 4x4 or 8x8 block on dense_q, under `controls`
+	Dense,         // 4x4 or 8x8 block on dense_q, under `controls`
+	Block          // fused block: dense 2^m x 2^m matrix on block_q (ascending), no controls
 };
 
 struct CompiledGate {
@@ -31,6 +32,9 @@ struct CompiledGate {
 	uint32_t dense_q[3] = {0, 0, 0};  // qubit of matrix bit 0, 1, 2
 	double dense_m[128];
 	std::complex<double> scale{1.0, 0.0};  // global factor taken out of the matrix
+	std::vector<uint32_t> block_q;          // Block: qubits, ascending (matrix bit j <-> block_q[j])
+	std::vector<std::complex<double>> block_m;  // Block: row-major 2^m x 2^m
+	uint32_t block_gates = 0;               // Block: original gates folded in
 
 	// qubits whose bit a tile must hold locally to apply this gate (targets of non-diagonal blocks)
 	uint64_t local_mask() const;

@@ -6,6 +6,7 @@
 #include <complex>
 #include <cstddef>
 #include <string>
+#include <vector>
 
 #include "qcs_gpu.h"
 
@@ -91,6 +92,11 @@ struct qcs_register {
 	std::complex<double> scale{1.0, 0.0};  // amplitudes = scale * stored values
 	void* batch = nullptr;                 // planner buffers (batch.cu)
 	int batch_mode = 1;                    // QCS_OPT_PASSES
+	int fusion = -1;                       // QCS_OPT_FUSION (-1: by precision)
+	int fusion_max = 5;                    // QCS_OPT_FUSION_MAX_QUBITS
+	double (*cost_model)(const std::vector<uint32_t>&, uint32_t, int, void*) = nullptr;  // learned block cost
+	void* cost_ctx = nullptr;
+	size_t last_blocks = 0;                // blocks of the last fused gate list
 	void* prof = nullptr;                  // launch timing records (profile.cu), when enabled
 	std::string err;
 	size_t amp_bytes() const { return prec == QCS_FP64 ? 16 : 8; }

@@ -8,7 +8,8 @@
 
 namespace qcs {
 
-enum class TKind : uint8_t { Ctrl1q = 0, Swap = 1, Dense2 = 2, Dense3 = 3, GlobalDiag = 4 };
+// DenseN: a fused block's 2^nins x 2^nins matrix whose bit j is the j-th inserted position
+enum class TKind : uint8_t { Ctrl1q = 0, Swap = 1, Dense2 = 2, Dense3 = 3, GlobalDiag = 4, DenseN = 5 };
 
 // one gate inside a pass, in tile-local bit positions
 struct TileOp {

@@ -113,6 +113,45 @@ __device__ __forceinline__ void tile_dense(cplx_t<T>* sm, uint32_t items, const 
 	}
 }
 
+// fused block: 2^K x 2^K complex matrix, matrix bit j = the j-th (ascending) inserted local position
+template <typename T, int K>
+__device__ __forceinline__ void tile_denseN(cplx_t<T>* sm, uint32_t items, const OpRegs op, const cplx_t<T>* __restrict__ mats) {
+	constexpr int D = 1 << K;
+	uint32_t bits[K];
+#pragma unroll
+	for (int j = 0; j < K; ++j) bits[j] = 1u << ((op.ins >> (8 * j)) & 0xffu);
+	for (uint32_t i = threadIdx.x; i < items; i += blockDim.x) {
+		const uint32_t b = expand_local(i, op);
+		cplx_t<T> v[D];
+#pragma unroll
+		for (int c = 0; c < D; ++c) {
+			uint32_t x = b;
+#pragma unroll
+			for (int j = 0; j < K; ++j)
+				if ((c >> j) & 1) x |= bits[j];
+			v[c] = sm[x];
+		}
+#pragma unroll 1
+		for (int r = 0; r < D; ++r) {
+			T re = 0, im = 0;
+			const cplx_t<T>* row = mats + op.mat + r * D;
+#pragma unroll
+			for (int c = 0; c < D; ++c) {
+				const cplx_t<T> mm = row[c];
+				re = fma(mm.x, v[c].x, re);
+				re = fma(-mm.y, v[c].y, re);
+				im = fma(mm.x, v[c].y, im);
+				im = fma(mm.y, v[c].x, im);
+			}
+			uint32_t x = b;
+#pragma unroll
+			for (int j = 0; j < K; ++j)
+				if ((r >> j) & 1) x |= bits[j];
+			sm[x] = mk<T>(re, im);
+		}
+	}
+}
+
 template <typename T>
 __device__ __forceinline__ void tile_apply(cplx_t<T>* sm, int k, const TileOp& top, const cplx_t<T>* __restrict__ mats, uint64_t base) {
 	const OpRegs op{top.ins, top.nins, top.lset, top.lbit0, top.lbit1, top.lbit2, top.mat};
@@ -164,8 +203,24 @@ __device__ __forceinline__ void tile_apply(cplx_t<T>* sm, int k, const TileOp& t
 		}
 	} else if (kind == TKind::Dense2) {
 		tile_dense<T, 2>(sm, items, op, mats);
-	} else {
+	} else if (kind == TKind::Dense3) {
 		tile_dense<T, 3>(sm, items, op, mats);
+	} else if constexpr (sizeof(T) == 4) {
+		// fused blocks (the FP32 path)
+		switch (op.nins) {
+		case 1: tile_denseN<T, 1>(sm, items, op, mats); break;
+		case 2: tile_denseN<T, 2>(sm, items, op, mats); break;
+		case 3: tile_denseN<T, 3>(sm, items, op, mats); break;
+		case 4: tile_denseN<T, 4>(sm, items, op, mats); break;
+		default: tile_denseN<T, 5>(sm, items, op, mats); break;
+		}
+	} else {
+		switch (op.nins) {
+		case 1: tile_denseN<T, 1>(sm, items, op, mats); break;
+		case 2: tile_denseN<T, 2>(sm, items, op, mats); break;
+		case 3: tile_denseN<T, 3>(sm, items, op, mats); break;
+		default: tile_denseN<T, 4>(sm, items, op, mats); break;
+		}
 	}
 }
 

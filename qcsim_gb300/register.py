@@ -85,6 +85,12 @@ class QubitRegister:
         """gate lists as shared-memory passes (default) or one kernel per gate"""
         self._ck(self._lib.qcs_set_option(self._h, L.QCS_OPT_PASSES, int(bool(enabled))))
 
+    def set_fusion(self, mode: int, max_qubits: int | None = None) -> None:
+        """fuse gate lists into dense blocks: 0 off, 1 greedy, 2 learned partition (FP32 default: 1)"""
+        self._ck(self._lib.qcs_set_option(self._h, L.QCS_OPT_FUSION, int(mode)))
+        if max_qubits is not None:
+            self._ck(self._lib.qcs_set_option(self._h, L.QCS_OPT_FUSION_MAX_QUBITS, int(max_qubits)))
+
     def profile(self, enable: bool = True) -> None:
         """bracket every kernel launch of this register with CUDA events (see read_profile)"""
         self._ck(self._lib.qcs_profile_enable(self._h, int(bool(enable))))

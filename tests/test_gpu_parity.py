@@ -367,6 +367,37 @@ def test_qft_passes(Q):
     assert np.abs(got - oracle_state(n, circuits.qft_circuit(0, n - 1), v)).max() <= TOL
 
 
+@pytest.mark.parametrize("n,max_q", [(10, 5), (16, 5), (18, 3), (20, 4)])
+def test_fused_fp32(Q, n, max_q):
+    """the FP32 fused path (blocks of <= max_q qubits, one dense matrix each) against the FP64 oracle:
+    fidelity of the renormalised state within 1e-9, max amplitude error within 2e-6"""
+    from qcsim_gb300 import circuits
+    ops = circuits.layered_circuit(n, 10, seed=n, p3=0.05)
+    reg = Q.QubitRegister(n, seed=1, precision="fp32")
+    reg.set_fusion(1, max_q)
+    reg.ApplyGates(ops)
+    got = reg.getRegisterStorage()
+    want = oracle_state(n, ops)
+    assert np.abs(got - want).max() < 2e-6
+    got = got / np.linalg.norm(got)
+    assert 1 - abs(np.vdot(want, got)) ** 2 < 1e-9
+
+
+def test_fused_fp64(Q):
+    """fusion on an FP64 register (blocks of <= 4 qubits) stays within the FP64 tolerance"""
+    from qcsim_gb300 import circuits, gates as G
+    n = 17
+    r = np.random.default_rng(2)
+    ops = circuits.layered_circuit(n, 6, seed=5, p3=0.1, controlled_frac=0.1)
+    for code in sorted(G.BY_CODE):
+        g = G.make(code, *r.uniform(0, 2 * np.pi, 4))
+        ops.append((g, *[int(x) for x in r.choice(n, size=3, replace=False)]))
+    reg = Q.QubitRegister(n, seed=1)
+    reg.set_fusion(1, 4)
+    reg.ApplyGates(ops)
+    assert np.abs(reg.getRegisterStorage() - oracle_state(n, ops)).max() <= 1e-12
+
+
 def test_larger_register_properties(Q):
     """24 qubits: unitary circuits keep the norm; an inverse circuit returns the start state"""
     from qcsim_gb300 import circuits
