@@ -148,6 +148,33 @@ int qcs_restore_state_destructive(qcs_handle h);
 /* ExpectationValue (QubitRegister.h:646-660): <psi| G_n..G_1 |psi> for a gate list, state unchanged */
 int qcs_expectation(qcs_handle h, const qcs_gate* gates, size_t count, double* re_im_out);
 
+/* ---- batched QAOA (no reference counterpart as one call: the reference runs
+ * QAOAIsingSubalgorithm::Exec (IsingModel.h:557-567) on one register at a time, and samples <H>
+ * with RepeatedMeasure (IsingModel.h:569-578); here many instances of different sizes run in one
+ * persistent launch captured in a CUDA graph, and <H> is the exact sum over basis states) ---- */
+typedef struct qcs_qaoa_instance {
+	uint32_t n;             /* qubits (spins) */
+	uint32_t nedges;        /* couplings */
+	const uint32_t* edges;  /* 2 * nedges qubit indices (i, j), i != j */
+	const double* J;        /* nedges couplings (small integers) */
+	const double* h;        /* n fields */
+} qcs_qaoa_instance;
+typedef struct qcs_qaoa_batch* qcs_qaoa_batch_handle;
+/* allocates every instance's statevector (2^n amplitudes each) in one device buffer */
+int qcs_qaoa_batch_create(const qcs_qaoa_instance* instances, size_t count, uint32_t p, int precision, qcs_qaoa_batch_handle* out);
+/* gammas and betas: count x p, row per instance */
+int qcs_qaoa_batch_set_angles(qcs_qaoa_batch_handle b, const double* gammas, const double* betas);
+/* CTAs per thread-block cluster sharing one instance (1, 2, 4, 8 or 16; 0 before the first call: 8) */
+int qcs_qaoa_batch_set_cluster(qcs_qaoa_batch_handle b, int ctas);
+/* runs every instance from |0..0>: H on all qubits, then p layers; energies_out (count doubles) gets
+ * <H> = sum_x |psi_x|^2 E(x), E(x) = -(sum h_i s_i + sum J_ij s_i s_j) (IsingModel.h:106-119) */
+int qcs_qaoa_batch_run(qcs_qaoa_batch_handle b, double* energies_out);
+/* the final statevector of one instance, host complex<double>[2^n] */
+int qcs_qaoa_batch_state(qcs_qaoa_batch_handle b, size_t index, double* host_state);
+uint64_t qcs_qaoa_batch_amplitudes(qcs_qaoa_batch_handle b);
+const char* qcs_qaoa_batch_last_error(qcs_qaoa_batch_handle b);
+int qcs_qaoa_batch_destroy(qcs_qaoa_batch_handle b);
+
 /* ---- engine options ---- */
 enum qcs_option {
 	QCS_OPT_PASSES = 1,          /* 1 (default): gate lists run as shared-memory passes; 0: one kernel per gate */

@@ -96,6 +96,14 @@ SIGNATURES = {
     "qcs_restore_state": (_i, [_h]),
     "qcs_restore_state_destructive": (_i, [_h]),
     "qcs_expectation": (_i, [_h, C.c_void_p, _sz, _pd]),
+    "qcs_qaoa_batch_create": (_i, [C.c_void_p, _sz, _u32, _i, C.POINTER(_h)]),
+    "qcs_qaoa_batch_set_angles": (_i, [_h, _pd, _pd]),
+    "qcs_qaoa_batch_set_cluster": (_i, [_h, _i]),
+    "qcs_qaoa_batch_run": (_i, [_h, _pd]),
+    "qcs_qaoa_batch_state": (_i, [_h, _sz, _pd]),
+    "qcs_qaoa_batch_amplitudes": (_u64, [_h]),
+    "qcs_qaoa_batch_last_error": (C.c_char_p, [_h]),
+    "qcs_qaoa_batch_destroy": (_i, [_h]),
     "qcs_set_option": (_i, [_h, _i, _i]),
     "qcs_profile_enable": (_i, [_h, _i]),
     "qcs_profile_read": (_i, [_h, C.c_void_p, _i, C.POINTER(_i)]),
@@ -105,6 +113,11 @@ SIGNATURES = {
     "qcs_rng_uniform": (_i, [_h, _pd, _sz]),
 }
 
+
+
+class qcs_qaoa_instance(C.Structure):
+    _fields_ = [("n", C.c_uint32), ("nedges", C.c_uint32), ("edges", C.POINTER(C.c_uint32)),
+                ("J", C.POINTER(C.c_double)), ("h", C.POINTER(C.c_double))]
 
 
 class qcs_profile_entry(C.Structure):

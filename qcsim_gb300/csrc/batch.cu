@@ -89,6 +89,34 @@ template <typename T> void push_mat2(std::vector<cplx_t<T>>& mats, const Mat2<do
 	}
 }
 
+// host check of one tile operation: inserted positions strictly ascending and below k, the bits it
+// reads or forces inside the inserted set, its matrix entries inside the table
+bool op_in_bounds(const TileOp& op, int k, size_t mats) {
+	if (op.nins > 8 || static_cast<int>(op.nins) > k) return false;
+	uint32_t insmask = 0;
+	int prev = -1;
+	for (int j = 0; j < op.nins; ++j) {
+		const int b = static_cast<int>((op.ins >> (8 * j)) & 0xffu);
+		if (b <= prev || b >= k) return false;
+		prev = b;
+		insmask |= 1u << b;
+	}
+	if ((op.lset & ~insmask) != 0) return false;
+	const bool flag0 = static_cast<TKind>(op.kind) == TKind::GlobalDiag;  // lbit0 is a side flag there
+	for (uint32_t bit : {flag0 ? 0u : op.lbit0, op.lbit1, op.lbit2})
+		if ((bit & ~insmask) != 0 || (bit & (bit - 1)) != 0) return false;
+	size_t need = 0;
+	switch (static_cast<TKind>(op.kind)) {
+	case TKind::Ctrl1q: case TKind::GlobalDiag: need = 4; break;
+	case TKind::Swap: need = 0; break;
+	case TKind::Dense2: need = 16; break;
+	case TKind::Dense3: need = 64; break;
+	case TKind::DenseN: need = size_t(1) << (2 * op.nins); break;
+	default: return false;
+	}
+	return op.mat + need <= mats;
+}
+
 template <typename T>
 int run_planned(qcs_handle h, const std::vector<PlannedPass>& passes, int kmax, int L0) {
 	const int n = static_cast<int>(h->n);
@@ -182,11 +210,23 @@ int run_planned(qcs_handle h, const std::vector<PlannedPass>& passes, int kmax, 
 			}
 			std::sort(ins.begin(), ins.end());
 			op.nins = static_cast<uint8_t>(ins.size());
-			for (size_t i = 0; i < ins.size(); ++i) op.ins |= static_cast<uint32_t>(ins[i]) << (8 * i);
+			for (size_t i = 0; i < ins.size(); ++i) op.ins |= static_cast<uint64_t>(ins[i]) << (8 * i);
 			ops.push_back(op);
 		}
 		tp.op_count = static_cast<uint32_t>(ops.size()) - tp.op_begin;
 		tps.push_back(tp);
+	}
+	// every index a kernel will form stays inside its tile and every matrix read inside the table
+	for (const TilePass& tp : tps) {
+		if (tp.k < 1 || tp.k > tile_qubits<T>() || tp.L > tp.k || tp.k - tp.L > 8 || tp.nfixed + tp.k != n) {
+			h->err = "apply gates: internal error (tile geometry)";
+			return QCS_CUDA_ERROR;
+		}
+		for (uint32_t i = tp.op_begin; i < tp.op_begin + tp.op_count; ++i)
+			if (!op_in_bounds(ops[i], tp.k, mats.size())) {
+				h->err = "apply gates: internal error (tile operation out of range)";
+				return QCS_CUDA_ERROR;
+			}
 	}
 	BatchBuffers* bb = static_cast<BatchBuffers*>(h->batch);
 	if (!bb) {

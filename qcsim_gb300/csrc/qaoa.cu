@@ -1,0 +1,600 @@
+// Batched QAOA: many Ising instances of different sizes, all statevectors resident in HBM, every
+// layer of every instance in one persistent kernel launch (replayed from a CUDA graph).
+//
+// The circuit is the reference's QAOAIsingSubalgorithm::Exec (IsingModel.h:557-567): H on every
+// qubit, then per layer the Ising operator -- CNOT(i<-j) RZ(2 gamma J_ij)(i) CNOT(i<-j) per edge and
+// RZ(gamma h_i) per field (IsingModel.h:491-531) -- and the mixer RX(2 beta) on every qubit
+// (:533-554).  The Ising operator is diagonal: amplitude x gets exp(-i gamma (K(x) + sum_q h_q s_q / 2))
+// with s = +1 for a 0 bit and K(x) = sum_ij J_ij s_i s_j.  With integer J, exp(-i gamma K) comes from a
+// table over K; the field factor from two tables over the low and high qubit groups.  The mixer is
+// the factored RX of the per-gate kernels (one FMA per real component), its scalar kept per instance.
+// <H> = sum_x |psi_x|^2 E(x), E(x) = -(sum h_q s_q + sum J_ij s_i s_j) (IsingModel.h:106-119, 203-206),
+// is reduced in FP64 in a fixed order.
+//
+// Work split: instances sorted by size (largest first) are dealt round-robin to thread-block
+// clusters; the CTAs of a cluster share an instance's tiles and meet at a cluster barrier between
+// passes.  No CTA waits on another cluster, so the kernel needs no inter-CTA flags.
+#include <algorithm>
+#include <cmath>
+#include <complex>
+#include <cstring>
+#include <numeric>
+#include <string>
+#include <vector>
+
+#include <cooperative_groups.h>
+
+#include "engine.cuh"
+#include "gate_math.cuh"
+
+namespace cg = cooperative_groups;
+
+namespace qcs {
+namespace {
+
+constexpr int kQThreads = 512;
+constexpr int kGroupBits = 12;   // tile / table group size
+constexpr int kMaxEdges = 64;
+constexpr int kMaxK = 192;       // |K| bound for the table over K (integer couplings)
+constexpr int kMaxLayers = 16;
+
+struct QInst {
+	uint64_t offset;       // first amplitude in the batch buffer
+	uint64_t part_offset;  // first energy partial
+	uint32_t n, nedges;
+	uint32_t g0;           // low group bits = min(n, 12)
+	uint32_t kmax;         // sum |J|
+	uint32_t tab;          // complex-table offset: per layer [2*kmax+1] + [2^g0] + [2^(n-g0)]
+	uint32_t eh;           // double-table offset: [2^g0] + [2^(n-g0)] field energies
+	uint8_t ei[kMaxEdges], ej[kMaxEdges];
+	int8_t J[kMaxEdges];
+	uint32_t tab_stride;   // complex entries per layer
+	uint32_t pad;
+};
+
+struct QLayer {
+	double x0, x1;  // factored RX coefficients
+	int form;       // 0: UnitIm01, 1: UnitIm10
+	int pad;
+};
+
+template <typename T> struct QParams {
+	cplx_t<T>* amps;
+	const QInst* inst;
+	const uint32_t* order;        // instance indices, largest first
+	uint32_t ninst;
+	uint32_t p;
+	const cplx_t<T>* tabs;
+	const double* etab;
+	const QLayer* layers;         // [inst][layer]
+	double* parts;                // energy partials
+	double* energies;             // out
+	double* scale2;               // |scale|^2 per instance
+};
+
+// tile of the pass: qubits 0..L-1 and `nh` high qubits starting at `hq0`; the other qubits index tiles
+struct TileGeo {
+	uint32_t L, hq0, nh, n;
+	__device__ uint64_t addr(uint64_t tile, uint32_t j) const {
+		const uint64_t low = j & ((1u << L) - 1);
+		const uint64_t high = static_cast<uint64_t>(j >> L) << hq0;
+		// tile bits fill the positions outside [0, L) and [hq0, hq0 + nh)
+		const uint32_t gap = hq0 - L;  // qubits L..hq0-1
+		const uint64_t tmid = tile & ((1ULL << gap) - 1);
+		const uint64_t thigh = tile >> gap;
+		return low | (tmid << L) | high | (thigh << (hq0 + nh));
+	}
+	__device__ uint64_t ntiles() const { return 1ULL << (n - L - nh); }
+	__device__ uint32_t size() const { return 1u << (L + nh); }
+};
+
+template <typename T>
+__device__ void rx_local(cplx_t<T>* sm, uint32_t k, uint32_t lo, uint32_t hi, const QLayer& L) {
+	// RX on local bits lo..hi-1 of a 2^k tile
+	Mat2<T> m;
+	m.m00 = mk<T>(1, static_cast<T>(L.x0));
+	m.m01 = mk<T>(1, static_cast<T>(L.x1));
+	const uint32_t items = (1u << k) >> 1;
+	for (uint32_t b = lo; b < hi; ++b) {
+		const uint32_t bit = 1u << b;
+		for (uint32_t i = threadIdx.x; i < items; i += blockDim.x) {
+			const uint32_t i0 = ((i >> b) << (b + 1)) | (i & (bit - 1));
+			cplx_t<T> a0 = sm[i0], a1 = sm[i0 | bit];
+			if (L.form == 0) op2<T, Op1::UnitIm01, 0>(a0, a1, m);
+			else op2<T, Op1::UnitIm10, 0>(a0, a1, m);
+			sm[i0] = a0;
+			sm[i0 | bit] = a1;
+		}
+		__syncthreads();
+	}
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kQThreads) k_qaoa(QParams<T> P) {
+	extern __shared__ __align__(16) unsigned char smraw[];
+	cplx_t<T>* sm = reinterpret_cast<cplx_t<T>*>(smraw);
+	__shared__ double red[kQThreads];
+	cg::cluster_group cluster = cg::this_cluster();
+	const uint32_t crank = cluster.block_rank();
+	const uint32_t csize = cluster.num_blocks();
+	const uint32_t nclusters = gridDim.x / csize;
+	const uint32_t cid = blockIdx.x / csize;
+	for (uint32_t w = cid; w < P.ninst; w += nclusters) {
+		const QInst& I = P.inst[P.order[w]];
+		cplx_t<T>* s = P.amps + I.offset;
+		const uint32_t n = I.n;
+		const uint32_t g0 = I.g0;
+		const uint32_t nstages = (n > g0) ? ((n - g0 + 5) / 6) : 0;  // high-qubit mixer passes
+		double partial_total = 0;
+		for (uint32_t l = 0; l < P.p; ++l) {
+			const QLayer Lr = P.layers[static_cast<size_t>(P.order[w]) * P.p + l];
+			const cplx_t<T>* tabJ = P.tabs + I.tab + static_cast<size_t>(l) * I.tab_stride;
+			const cplx_t<T>* tab0 = tabJ + (2 * I.kmax + 1);
+			const cplx_t<T>* tab1 = tab0 + (1u << g0);
+			const bool last_layer = (l + 1 == P.p);
+			for (uint32_t stage = 0; stage <= nstages; ++stage) {
+				TileGeo G;
+				G.n = n;
+				if (stage == 0) {
+					G.L = g0; G.hq0 = g0; G.nh = 0;
+				} else {
+					const uint32_t lo = g0 + 6 * (stage - 1);
+					G.L = 6; G.hq0 = lo; G.nh = min(6u, n - lo);
+				}
+				const uint64_t ntiles = G.ntiles();
+				const uint32_t K = G.size();
+				const bool final_pass = last_layer && stage == nstages;
+				for (uint64_t t = crank; t < ntiles; t += csize) {
+					for (uint32_t j = threadIdx.x; j < K; j += blockDim.x) sm[j] = s[G.addr(t, j)];
+					__syncthreads();
+					if (stage == 0) {
+						// the Ising operator on every amplitude of the tile, then RX on the low qubits
+						for (uint32_t j = threadIdx.x; j < K; j += blockDim.x) {
+							const uint64_t x = G.addr(t, j);
+							int kk = 0;
+							for (uint32_t e = 0; e < I.nedges; ++e) {
+								const int par = static_cast<int>(((x >> I.ei[e]) ^ (x >> I.ej[e])) & 1ULL);
+								kk += par ? -I.J[e] : I.J[e];
+							}
+							cplx_t<T> f = cmul<T>(tabJ[kk + static_cast<int>(I.kmax)], tab0[x & ((1u << g0) - 1)]);
+							f = cmul<T>(f, tab1[x >> g0]);
+							sm[j] = cmul<T>(sm[j], f);
+						}
+						__syncthreads();
+						rx_local<T>(sm, G.L, 0, G.L, Lr);
+					} else {
+						rx_local<T>(sm, G.L + G.nh, G.L, G.L + G.nh, Lr);
+					}
+					if (final_pass) {
+						// <H> partial of this tile: sum |a|^2 E(x)
+						double acc = 0;
+						const double* eh0 = P.etab + I.eh;
+						const double* eh1 = eh0 + (1u << g0);
+						for (uint32_t j = threadIdx.x; j < K; j += blockDim.x) {
+							const uint64_t x = G.addr(t, j);
+							int kk = 0;
+							for (uint32_t e = 0; e < I.nedges; ++e) {
+								const int par = static_cast<int>(((x >> I.ei[e]) ^ (x >> I.ej[e])) & 1ULL);
+								kk += par ? -I.J[e] : I.J[e];
+							}
+							const double E = -(static_cast<double>(kk) + eh0[x & ((1u << g0) - 1)] + eh1[x >> g0]);
+							const double ax = sm[j].x, ay = sm[j].y;
+							acc += (ax * ax + ay * ay) * E;
+						}
+						red[threadIdx.x] = acc;
+						__syncthreads();
+						for (int wdt = blockDim.x / 2; wdt > 0; wdt >>= 1) {
+							if (threadIdx.x < wdt) red[threadIdx.x] += red[threadIdx.x + wdt];
+							__syncthreads();
+						}
+						if (threadIdx.x == 0) P.parts[I.part_offset + t] = red[0];
+						__syncthreads();
+					}
+					for (uint32_t j = threadIdx.x; j < K; j += blockDim.x) s[G.addr(t, j)] = sm[j];
+					__syncthreads();
+				}
+				cluster.sync();
+				(void)partial_total;
+			}
+		}
+		// fixed-order final reduction by the cluster's first CTA
+		if (crank == 0) {
+			TileGeo G;
+			G.n = n;
+			if (nstages == 0) { G.L = g0; G.hq0 = g0; G.nh = 0; }
+			else {
+				const uint32_t lo = g0 + 6 * (nstages - 1);
+				G.L = 6; G.hq0 = lo; G.nh = min(6u, n - lo);
+			}
+			const uint64_t ntiles = G.ntiles();
+			double acc = 0;
+			for (uint64_t t = threadIdx.x; t < ntiles; t += blockDim.x) acc += P.parts[I.part_offset + t];
+			red[threadIdx.x] = acc;
+			__syncthreads();
+			for (int wdt = blockDim.x / 2; wdt > 0; wdt >>= 1) {
+				if (threadIdx.x < wdt) red[threadIdx.x] += red[threadIdx.x + wdt];
+				__syncthreads();
+			}
+			if (threadIdx.x == 0) P.energies[P.order[w]] = red[0] * P.scale2[P.order[w]];
+			__syncthreads();
+		}
+		cluster.sync();
+	}
+}
+
+}  // namespace
+}  // namespace qcs
+
+using cd = std::complex<double>;
+
+struct qcs_qaoa_batch {
+	int prec = QCS_FP64;
+	uint32_t p = 0;
+	size_t count = 0;
+	std::vector<qcs::QInst> inst;
+	std::vector<std::vector<double>> h;      // fields per instance
+	std::vector<uint32_t> order;
+	uint64_t total_amps = 0, total_parts = 0;
+	size_t tab_entries = 0, etab_entries = 0;
+	void* d_amps = nullptr;
+	qcs::QInst* d_inst = nullptr;
+	uint32_t* d_order = nullptr;
+	void* d_tabs = nullptr;
+	double* d_etab = nullptr;
+	qcs::QLayer* d_layers = nullptr;
+	double* d_parts = nullptr;
+	double* d_energies = nullptr;
+	double* d_scale2 = nullptr;
+	double* h_energies = nullptr;  // pinned
+	std::vector<cd> scale;         // complex scale per instance (amplitudes = scale * stored)
+	cudaStream_t stream = nullptr;
+	cudaGraph_t graph = nullptr;
+	cudaGraphExec_t exec = nullptr;
+	int cluster = 0;               // CTAs per cluster (0: choose)
+	int sms = 148;
+	std::string err;
+};
+
+namespace {
+
+int qfail(qcs_qaoa_batch* b, int st, const std::string& m) {
+	if (b) b->err = m;
+	return st;
+}
+
+template <typename T> typename qcs::cplx_t<T> cc(const cd& v) {
+	typename qcs::cplx_t<T> r;
+	r.x = static_cast<T>(v.real());
+	r.y = static_cast<T>(v.imag());
+	return r;
+}
+
+template <typename T>
+cudaError_t launch(qcs_qaoa_batch* b) {
+	qcs::QParams<T> P;
+	P.amps = static_cast<qcs::cplx_t<T>*>(b->d_amps);
+	P.inst = b->d_inst;
+	P.order = b->d_order;
+	P.ninst = static_cast<uint32_t>(b->count);
+	P.p = b->p;
+	P.tabs = static_cast<const qcs::cplx_t<T>*>(b->d_tabs);
+	P.etab = b->d_etab;
+	P.layers = b->d_layers;
+	P.parts = b->d_parts;
+	P.energies = b->d_energies;
+	P.scale2 = b->d_scale2;
+	const size_t smem = (size_t(1) << qcs::kGroupBits) * sizeof(qcs::cplx_t<T>);
+	cudaError_t e = cudaFuncSetAttribute(qcs::k_qaoa<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+	if (e == cudaSuccess) e = cudaFuncSetAttribute(qcs::k_qaoa<T>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+	if (e != cudaSuccess) return e;
+	const int csize = b->cluster > 0 ? b->cluster : 8;
+	int per_sm = static_cast<int>((200 * 1024) / (smem + 8192));
+	per_sm = std::max(1, std::min(per_sm, 3));
+	int grid = (b->sms * per_sm / csize) * csize;
+	if (grid < csize) grid = csize;
+	cudaLaunchConfig_t cfg = {};
+	cfg.gridDim = dim3(static_cast<unsigned>(grid));
+	cfg.blockDim = dim3(qcs::kQThreads);
+	cfg.dynamicSmemBytes = smem;
+	cfg.stream = b->stream;
+	cudaLaunchAttribute attr[1];
+	attr[0].id = cudaLaunchAttributeClusterDimension;
+	attr[0].val.clusterDim.x = static_cast<unsigned>(csize);
+	attr[0].val.clusterDim.y = 1;
+	attr[0].val.clusterDim.z = 1;
+	cfg.attrs = attr;
+	cfg.numAttrs = 1;
+	e = cudaLaunchKernelEx(&cfg, qcs::k_qaoa<T>, P);
+	qcs::note_launches(1);
+	return e;
+}
+
+cudaError_t record(qcs_qaoa_batch* b) {
+	// initial state H^n|0>: every amplitude (1/sqrt2)^n, as the reference's n Hadamards produce it
+	cudaError_t e = cudaSuccess;
+	for (size_t i = 0; i < b->count && e == cudaSuccess; ++i) {
+		const qcs::QInst& I = b->inst[i];
+		double v = 1.0;
+		const double r2 = 1. / std::sqrt(2.);
+		for (uint32_t q = 0; q < I.n; ++q) v *= r2;
+		const uint64_t N = 1ULL << I.n;
+		e = b->prec == QCS_FP64 ? qcs::launch_fill_const<double>(static_cast<double2*>(b->d_amps) + I.offset, N, v, 0, b->stream)
+		                        : qcs::launch_fill_const<float>(static_cast<float2*>(b->d_amps) + I.offset, N, v, 0, b->stream);
+	}
+	if (e == cudaSuccess) e = b->prec == QCS_FP64 ? launch<double>(b) : launch<float>(b);
+	if (e == cudaSuccess)
+		e = cudaMemcpyAsync(b->h_energies, b->d_energies, b->count * sizeof(double), cudaMemcpyDeviceToHost, b->stream);
+	return e;
+}
+
+}  // namespace
+
+extern "C" {
+
+int qcs_qaoa_batch_create(const qcs_qaoa_instance* instances, size_t count, uint32_t p, int precision, qcs_qaoa_batch_handle* out) {
+	if (!instances || !out || count == 0 || p == 0 || p > static_cast<uint32_t>(qcs::kMaxLayers)) return QCS_INVALID_ARGUMENT;
+	if (precision != QCS_FP64 && precision != QCS_FP32) return QCS_INVALID_ARGUMENT;
+	*out = nullptr;
+	auto* b = new qcs_qaoa_batch;
+	b->prec = precision;
+	b->p = p;
+	b->count = count;
+	b->inst.resize(count);
+	b->h.resize(count);
+	b->scale.assign(count, cd(1, 0));
+	for (size_t i = 0; i < count; ++i) {
+		const qcs_qaoa_instance& in = instances[i];
+		qcs::QInst& I = b->inst[i];
+		std::memset(&I, 0, sizeof(I));
+		if (in.n < 2 || in.n > 30 || in.nedges > static_cast<uint32_t>(qcs::kMaxEdges)) {
+			delete b;
+			return QCS_UNSUPPORTED;
+		}
+		I.n = in.n;
+		I.nedges = in.nedges;
+		I.g0 = std::min<uint32_t>(in.n, qcs::kGroupBits);
+		int ksum = 0;
+		for (uint32_t e = 0; e < in.nedges; ++e) {
+			const double J = in.J[e];
+			if (J != std::floor(J) || std::abs(J) > 16 || in.edges[2 * e] >= in.n || in.edges[2 * e + 1] >= in.n ||
+			    in.edges[2 * e] == in.edges[2 * e + 1]) {
+				delete b;
+				return QCS_UNSUPPORTED;  // the batch kernel takes small integer couplings
+			}
+			I.ei[e] = static_cast<uint8_t>(in.edges[2 * e]);
+			I.ej[e] = static_cast<uint8_t>(in.edges[2 * e + 1]);
+			I.J[e] = static_cast<int8_t>(J);
+			ksum += static_cast<int>(std::abs(J));
+		}
+		if (ksum > qcs::kMaxK) {
+			delete b;
+			return QCS_UNSUPPORTED;
+		}
+		I.kmax = static_cast<uint32_t>(ksum);
+		b->h[i].assign(in.h, in.h + in.n);
+		I.offset = b->total_amps;
+		b->total_amps += 1ULL << in.n;
+		I.tab_stride = (2 * I.kmax + 1) + (1u << I.g0) + (1u << (in.n - I.g0));
+		I.tab = static_cast<uint32_t>(b->tab_entries);
+		b->tab_entries += static_cast<size_t>(I.tab_stride) * p;
+		I.eh = static_cast<uint32_t>(b->etab_entries);
+		b->etab_entries += (1u << I.g0) + (1u << (in.n - I.g0));
+		I.part_offset = b->total_parts;
+		// tiles of the final pass
+		const uint32_t nst = (I.n > I.g0) ? ((I.n - I.g0 + 5) / 6) : 0;
+		uint32_t L = I.g0, nh = 0;
+		if (nst) {
+			const uint32_t lo = I.g0 + 6 * (nst - 1);
+			L = 6;
+			nh = std::min(6u, I.n - lo);
+		}
+		b->total_parts += 1ULL << (I.n - L - nh);
+	}
+	b->order.resize(count);
+	std::iota(b->order.begin(), b->order.end(), 0u);
+	std::stable_sort(b->order.begin(), b->order.end(), [&](uint32_t a, uint32_t c) { return b->inst[a].n > b->inst[c].n; });
+	int dev = 0;
+	cudaGetDevice(&dev);
+	cudaDeviceGetAttribute(&b->sms, cudaDevAttrMultiProcessorCount, dev);
+	const size_t ab = b->prec == QCS_FP64 ? 16 : 8;
+	cudaError_t e = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking);
+	if (e == cudaSuccess) e = cudaMalloc(&b->d_amps, b->total_amps * ab);
+	if (e == cudaSuccess) e = cudaMalloc(&b->d_inst, count * sizeof(qcs::QInst));
+	if (e == cudaSuccess) e = cudaMalloc(&b->d_order, count * sizeof(uint32_t));
+	if (e == cudaSuccess) e = cudaMalloc(&b->d_tabs, b->tab_entries * ab);
+	if (e == cudaSuccess) e = cudaMalloc(&b->d_etab, b->etab_entries * sizeof(double));
+	if (e == cudaSuccess) e = cudaMalloc(&b->d_layers, count * p * sizeof(qcs::QLayer));
+	if (e == cudaSuccess) e = cudaMalloc(&b->d_parts, std::max<uint64_t>(1, b->total_parts) * sizeof(double));
+	if (e == cudaSuccess) e = cudaMalloc(&b->d_energies, count * sizeof(double));
+	if (e == cudaSuccess) e = cudaMalloc(&b->d_scale2, count * sizeof(double));
+	if (e == cudaSuccess) e = cudaMallocHost(&b->h_energies, count * sizeof(double));
+	if (e == cudaSuccess) e = cudaMemcpyAsync(b->d_inst, b->inst.data(), count * sizeof(qcs::QInst), cudaMemcpyHostToDevice, b->stream);
+	if (e == cudaSuccess) e = cudaMemcpyAsync(b->d_order, b->order.data(), count * sizeof(uint32_t), cudaMemcpyHostToDevice, b->stream);
+	// field energy tables: sum over the group's qubits of h_q s_q
+	if (e == cudaSuccess) {
+		std::vector<double> et(b->etab_entries);
+		for (size_t i = 0; i < count; ++i) {
+			const qcs::QInst& I = b->inst[i];
+			const uint32_t g1 = I.n - I.g0;
+			for (uint32_t x = 0; x < (1u << I.g0); ++x) {
+				double s = 0;
+				for (uint32_t q = 0; q < I.g0; ++q) s += b->h[i][q] * (((x >> q) & 1u) ? -1.0 : 1.0);
+				et[I.eh + x] = s;
+			}
+			for (uint32_t x = 0; x < (1u << g1); ++x) {
+				double s = 0;
+				for (uint32_t q = 0; q < g1; ++q) s += b->h[i][I.g0 + q] * (((x >> q) & 1u) ? -1.0 : 1.0);
+				et[I.eh + (1u << I.g0) + x] = s;
+			}
+		}
+		e = cudaMemcpy(b->d_etab, et.data(), et.size() * sizeof(double), cudaMemcpyHostToDevice);
+	}
+	if (e != cudaSuccess) {
+		qcs_qaoa_batch_destroy(b);
+		cudaGetLastError();
+		return e == cudaErrorMemoryAllocation ? QCS_OUT_OF_MEMORY : QCS_CUDA_ERROR;
+	}
+	*out = b;
+	return QCS_OK;
+}
+
+int qcs_qaoa_batch_set_angles(qcs_qaoa_batch_handle b, const double* gammas, const double* betas) {
+	if (!b || !gammas || !betas) return QCS_INVALID_ARGUMENT;
+	const size_t ab = b->prec == QCS_FP64 ? 16 : 8;
+	std::vector<unsigned char> tabs(b->tab_entries * ab);
+	std::vector<qcs::QLayer> layers(b->count * b->p);
+	std::vector<double> s2(b->count);
+	auto put = [&](size_t idx, const cd& v) {
+		if (b->prec == QCS_FP64) {
+			const double2 x = make_double2(v.real(), v.imag());
+			std::memcpy(&tabs[idx * ab], &x, ab);
+		} else {
+			const float2 x = make_float2(static_cast<float>(v.real()), static_cast<float>(v.imag()));
+			std::memcpy(&tabs[idx * ab], &x, ab);
+		}
+	};
+	for (size_t i = 0; i < b->count; ++i) {
+		const qcs::QInst& I = b->inst[i];
+		cd scale(1, 0);  // H^n is in the initial amplitudes; the mixers' factored scalars accumulate here
+		for (uint32_t l = 0; l < b->p; ++l) {
+			const double g = gammas[i * b->p + l], be = betas[i * b->p + l];
+			const size_t base = I.tab + static_cast<size_t>(l) * I.tab_stride;
+			// exp(-i g K) for K in [-kmax, kmax]: each edge contributes exp(-i g J s_i s_j) (the CNOT-RZ-CNOT
+			// sandwich, RZ angle 2 g J)
+			for (int k = -static_cast<int>(I.kmax); k <= static_cast<int>(I.kmax); ++k)
+				put(base + static_cast<size_t>(k + static_cast<int>(I.kmax)), std::polar(1.0, -g * k));
+			// field factors: RZ(g h_q) gives exp(-i g h_q s_q / 2)
+			const uint32_t g1 = I.n - I.g0;
+			for (uint32_t x = 0; x < (1u << I.g0); ++x) {
+				cd f(1, 0);
+				for (uint32_t q = 0; q < I.g0; ++q) {
+					const double hq = b->h[i][q];
+					if (hq == 0.) continue;  // the reference skips zero fields (IsingModel.h:522)
+					f *= std::polar(1.0, (((x >> q) & 1u) ? 0.5 : -0.5) * g * hq);
+				}
+				put(base + 2 * I.kmax + 1 + x, f);
+			}
+			for (uint32_t x = 0; x < (1u << g1); ++x) {
+				cd f(1, 0);
+				for (uint32_t q = 0; q < g1; ++q) {
+					const double hq = b->h[i][I.g0 + q];
+					if (hq == 0.) continue;
+					f *= std::polar(1.0, (((x >> q) & 1u) ? 0.5 : -0.5) * g * hq);
+				}
+				put(base + 2 * I.kmax + 1 + (1u << I.g0) + x, f);
+			}
+			// mixer RX(2 beta) = [[c, -is], [-is, c]] with c = cos(beta), s = sin(beta) (SimpleGates.h:840-848),
+			// factored like the per-gate kernels
+			const double c = std::cos(be), s = std::sin(be);
+			qcs::QLayer& L = layers[i * b->p + l];
+			std::memset(&L, 0, sizeof(L));
+			if (std::abs(c) >= std::abs(s)) {
+				L.form = 0;
+				L.x0 = -s / c;
+				L.x1 = -s / c;
+				for (uint32_t q = 0; q < I.n; ++q) scale *= c;
+			} else {
+				L.form = 1;
+				L.x0 = c / s;
+				L.x1 = c / s;
+				for (uint32_t q = 0; q < I.n; ++q) scale *= cd(0, -s);
+			}
+		}
+		b->scale[i] = scale;
+		s2[i] = std::norm(scale);
+	}
+	cudaError_t e = cudaMemcpy(b->d_tabs, tabs.data(), tabs.size(), cudaMemcpyHostToDevice);
+	if (e == cudaSuccess) e = cudaMemcpy(b->d_layers, layers.data(), layers.size() * sizeof(qcs::QLayer), cudaMemcpyHostToDevice);
+	if (e == cudaSuccess) e = cudaMemcpy(b->d_scale2, s2.data(), s2.size() * sizeof(double), cudaMemcpyHostToDevice);
+	if (e != cudaSuccess) return qfail(b, QCS_CUDA_ERROR, std::string("set angles: ") + cudaGetErrorString(e));
+	return QCS_OK;
+}
+
+int qcs_qaoa_batch_set_cluster(qcs_qaoa_batch_handle b, int ctas) {
+	if (!b || ctas < 1 || ctas > 16 || (ctas & (ctas - 1))) return QCS_INVALID_ARGUMENT;
+	b->cluster = ctas;
+	if (b->exec) {
+		cudaGraphExecDestroy(b->exec);
+		b->exec = nullptr;
+	}
+	if (b->graph) {
+		cudaGraphDestroy(b->graph);
+		b->graph = nullptr;
+	}
+	return QCS_OK;
+}
+
+int qcs_qaoa_batch_run(qcs_qaoa_batch_handle b, double* energies_out) {
+	if (!b) return QCS_INVALID_ARGUMENT;
+	cudaError_t e = cudaSuccess;
+	if (!b->exec) {
+		e = cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal);
+		if (e == cudaSuccess) {
+			cudaError_t r = record(b);
+			e = cudaStreamEndCapture(b->stream, &b->graph);
+			if (r != cudaSuccess) e = r;
+		}
+		if (e == cudaSuccess) e = cudaGraphInstantiate(&b->exec, b->graph, 0);
+		if (e != cudaSuccess) {
+			cudaGetLastError();
+			return qfail(b, QCS_CUDA_ERROR, std::string("graph capture: ") + cudaGetErrorString(e));
+		}
+	}
+	e = cudaGraphLaunch(b->exec, b->stream);
+	if (e == cudaSuccess) e = cudaStreamSynchronize(b->stream);
+	if (e != cudaSuccess) return qfail(b, QCS_CUDA_ERROR, std::string("run: ") + cudaGetErrorString(e));
+	if (energies_out) std::memcpy(energies_out, b->h_energies, b->count * sizeof(double));
+	return QCS_OK;
+}
+
+int qcs_qaoa_batch_state(qcs_qaoa_batch_handle b, size_t index, double* host_state) {
+	if (!b || !host_state || index >= b->count) return QCS_INVALID_ARGUMENT;
+	const qcs::QInst& I = b->inst[index];
+	const uint64_t N = 1ULL << I.n;
+	const cd sc = b->scale[index];
+	cudaError_t e;
+	if (b->prec == QCS_FP64) {
+		e = cudaMemcpy(host_state, static_cast<double2*>(b->d_amps) + I.offset, N * 16, cudaMemcpyDeviceToHost);
+		for (uint64_t i = 0; i < N && e == cudaSuccess; ++i) {
+			const cd v = sc * cd(host_state[2 * i], host_state[2 * i + 1]);
+			host_state[2 * i] = v.real();
+			host_state[2 * i + 1] = v.imag();
+		}
+	} else {
+		std::vector<float> tmp(2 * N);
+		e = cudaMemcpy(tmp.data(), static_cast<float2*>(b->d_amps) + I.offset, N * 8, cudaMemcpyDeviceToHost);
+		for (uint64_t i = 0; i < N && e == cudaSuccess; ++i) {
+			const cd v = sc * cd(tmp[2 * i], tmp[2 * i + 1]);
+			host_state[2 * i] = v.real();
+			host_state[2 * i + 1] = v.imag();
+		}
+	}
+	if (e != cudaSuccess) return qfail(b, QCS_CUDA_ERROR, std::string("state: ") + cudaGetErrorString(e));
+	return QCS_OK;
+}
+
+uint64_t qcs_qaoa_batch_amplitudes(qcs_qaoa_batch_handle b) { return b ? b->total_amps : 0; }
+
+const char* qcs_qaoa_batch_last_error(qcs_qaoa_batch_handle b) { return b ? b->err.c_str() : "null handle"; }
+
+int qcs_qaoa_batch_destroy(qcs_qaoa_batch_handle b) {
+	if (!b) return QCS_INVALID_ARGUMENT;
+	if (b->stream) cudaStreamSynchronize(b->stream);
+	if (b->exec) cudaGraphExecDestroy(b->exec);
+	if (b->graph) cudaGraphDestroy(b->graph);
+	cudaFree(b->d_amps);
+	cudaFree(b->d_inst);
+	cudaFree(b->d_order);
+	cudaFree(b->d_tabs);
+	cudaFree(b->d_etab);
+	cudaFree(b->d_layers);
+	cudaFree(b->d_parts);
+	cudaFree(b->d_energies);
+	cudaFree(b->d_scale2);
+	if (b->h_energies) cudaFreeHost(b->h_energies);
+	if (b->stream) cudaStreamDestroy(b->stream);
+	delete b;
+	return QCS_OK;
+}
+
+}  // extern "C"

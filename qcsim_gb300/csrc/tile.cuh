@@ -15,9 +15,9 @@ enum class TKind : uint8_t { Ctrl1q = 0, Swap = 1, Dense2 = 2, Dense3 = 3, Globa
 struct TileOp {
 	uint8_t kind;      // TKind
 	uint8_t op;        // Op1 (Ctrl1q, GlobalDiag) or SwapKind (Swap)
-	uint8_t nins;      // number of local bit positions a work item does not enumerate
-	uint8_t pad;
-	uint32_t ins;      // those positions, ascending, 8 bits each (lowest byte first)
+	uint8_t nins;      // number of local bit positions a work item does not enumerate (at most 8)
+	uint8_t pad[5];
+	uint64_t ins;      // those positions, ascending, 8 bits each (lowest byte first)
 	uint32_t lset;     // local control bits (forced to one in every work item)
 	uint32_t lbit0;    // Ctrl1q: target bit (0 = the factor sits on the target-bit-0 half); Swap: bit A; Dense: matrix bit 0
 	uint32_t lbit1;    // Swap: bit B; Dense: matrix bit 1

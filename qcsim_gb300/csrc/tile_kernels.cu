@@ -12,13 +12,14 @@ constexpr int kMaxHigh = 8;  // at most 8 tile qubits above the contiguous low b
 
 // the loop-invariant fields of a TileOp, held in registers
 struct OpRegs {
-	uint32_t ins, nins, lset, lbit0, lbit1, lbit2, mat;
+	uint64_t ins;
+	uint32_t nins, lset, lbit0, lbit1, lbit2, mat;
 };
 
 __device__ __forceinline__ uint32_t expand_local(uint32_t i, const OpRegs& op) {
-	uint32_t packed = op.ins;
+	uint64_t packed = op.ins;
 	for (uint32_t j = 0; j < op.nins; ++j) {
-		const uint32_t b = packed & 0xffu;
+		const uint32_t b = static_cast<uint32_t>(packed & 0xffu);
 		packed >>= 8;
 		i = ((i >> b) << (b + 1)) | (i & ((1u << b) - 1));
 	}
@@ -119,7 +120,7 @@ __device__ __forceinline__ void tile_denseN(cplx_t<T>* sm, uint32_t items, const
 	constexpr int D = 1 << K;
 	uint32_t bits[K];
 #pragma unroll
-	for (int j = 0; j < K; ++j) bits[j] = 1u << ((op.ins >> (8 * j)) & 0xffu);
+	for (int j = 0; j < K; ++j) bits[j] = 1u << static_cast<uint32_t>((op.ins >> (8 * j)) & 0xffu);
 	for (uint32_t i = threadIdx.x; i < items; i += blockDim.x) {
 		const uint32_t b = expand_local(i, op);
 		cplx_t<T> v[D];

@@ -1,0 +1,72 @@
+"""Batched QAOA over the engine (qcs_qaoa_batch_* in include/qcs_gpu.h): many Ising instances of
+different sizes, all statevectors resident on the GPU, every layer in one persistent launch replayed
+from a CUDA graph.  The circuit per instance is QAOAIsingSubalgorithm::Exec (IsingModel.h:557-567);
+<H> is the exact expectation sum_x |psi_x|^2 E(x) (the reference estimates it from 100000 samples,
+IsingModel.h:569-578)."""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _lib as L
+
+
+class QaoaBatch:
+    def __init__(self, instances: list[dict], p: int, precision: str = "fp64"):
+        self._lib = L.load()
+        self.instances = instances
+        self.p = p
+        self._keep = []
+        arr = (L.qcs_qaoa_instance * len(instances))()
+        for i, inst in enumerate(instances):
+            e = np.ascontiguousarray(np.array(inst["edges"], dtype=np.uint32).reshape(-1))
+            J = np.ascontiguousarray(inst["J"], dtype=np.float64)
+            h = np.ascontiguousarray(inst["h"], dtype=np.float64)
+            self._keep += [e, J, h]
+            arr[i].n = inst["n"]
+            arr[i].nedges = len(inst["edges"])
+            arr[i].edges = e.ctypes.data_as(C.POINTER(C.c_uint32))
+            arr[i].J = J.ctypes.data_as(C.POINTER(C.c_double))
+            arr[i].h = h.ctypes.data_as(C.POINTER(C.c_double))
+        self._h = C.c_void_p()
+        prec = L.QCS_FP64 if precision == "fp64" else L.QCS_FP32
+        L.check(self._lib.qcs_qaoa_batch_create(C.cast(arr, C.c_void_p), len(instances), p, prec, C.byref(self._h)))
+        self.set_angles(np.array([inst["gammas"] for inst in instances]), np.array([inst["betas"] for inst in instances]))
+
+    def _ck(self, st: int) -> None:
+        if st != L.QCS_OK:
+            raise L.QcsError(st, self._lib.qcs_qaoa_batch_last_error(self._h).decode())
+
+    def set_angles(self, gammas: np.ndarray, betas: np.ndarray) -> None:
+        g = np.ascontiguousarray(gammas, dtype=np.float64)
+        b = np.ascontiguousarray(betas, dtype=np.float64)
+        self._ck(self._lib.qcs_qaoa_batch_set_angles(self._h, L.dptr(g), L.dptr(b)))
+
+    def set_cluster(self, ctas: int) -> None:
+        self._ck(self._lib.qcs_qaoa_batch_set_cluster(self._h, ctas))
+
+    def run(self) -> np.ndarray:
+        out = np.empty(len(self.instances), dtype=np.float64)
+        self._ck(self._lib.qcs_qaoa_batch_run(self._h, L.dptr(out)))
+        return out
+
+    def state(self, i: int) -> np.ndarray:
+        out = np.empty(1 << self.instances[i]["n"], dtype=np.complex128)
+        self._ck(self._lib.qcs_qaoa_batch_state(self._h, i, out.view(np.float64).ctypes.data_as(C.POINTER(C.c_double))))
+        return out
+
+    @property
+    def amplitudes(self) -> int:
+        return int(self._lib.qcs_qaoa_batch_amplitudes(self._h))
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            self._lib.qcs_qaoa_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
