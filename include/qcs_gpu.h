@@ -175,6 +175,38 @@ uint64_t qcs_qaoa_batch_amplitudes(qcs_qaoa_batch_handle b);
 const char* qcs_qaoa_batch_last_error(qcs_qaoa_batch_handle b);
 int qcs_qaoa_batch_destroy(qcs_qaoa_batch_handle b);
 
+/* ---- dense operators on a few qubits (the kernel of the fused path; NQubitsQuantumGate-style
+ * operators, NQubitsQuantumGate.h:27-47, without building the 2^n x 2^n matrix) ----
+ * m: 2^k x 2^k complex, row-major interleaved; matrix bit j is qubits[j] (any order, distinct);
+ * k <= 5 (FP32 registers) or 4 (FP64 registers) */
+int qcs_apply_matrix(qcs_handle h, const uint32_t* qubits, uint32_t k, const double* m);
+
+/* ---- learned cost model (no reference counterpart): a 3-layer MLP, F inputs -> 64 -> 64 -> 1 with
+ * ReLU, FP32, trained and evaluated by the engine's own kernels.  It predicts the log of a fused
+ * block's device time; a register in fusion mode 2 scores candidate partitions with it. ---- */
+typedef struct qcs_mlp* qcs_mlp_handle;
+int qcs_mlp_create(int inputs, uint64_t seed, qcs_mlp_handle* out);
+int qcs_mlp_destroy(qcs_mlp_handle m);
+int qcs_mlp_num_params(qcs_mlp_handle m);
+/* parameters as W1[64][F], b1[64], W2[64][64], b2[64], W3[64], b3 */
+int qcs_mlp_get_params(qcs_mlp_handle m, float* out);
+int qcs_mlp_set_params(qcs_mlp_handle m, const float* in);
+/* x: count x F row-major */
+int qcs_mlp_predict(qcs_mlp_handle m, const float* x, int count, float* y_out);
+/* gradient of mean((y - t)^2) over the batch, and that loss */
+int qcs_mlp_gradient(qcs_mlp_handle m, const float* x, const float* t, int count, float* grad_out, float* loss_out);
+/* `steps` full-batch Adam steps with learning rate lr; the loss after the last step */
+int qcs_mlp_train(qcs_mlp_handle m, const float* x, const float* t, int count, int steps, float lr, float* loss_out);
+/* the model's input vector for a block: register qubits, the block's qubits (ascending), gate count */
+int qcs_block_features(uint32_t nqubits, const uint32_t* qubits, uint32_t k, uint32_t ngates, float* out);
+/* the greedy fuser's partition of a gate list (host only, no GPU): per block its qubit mask and the
+ * number of gates folded in; nblocks_out may exceed capacity (then only capacity entries are written) */
+int qcs_fusion_plan(uint32_t nqubits, const qcs_gate* gates, size_t count, int max_qubits, uint64_t* block_masks,
+                    uint32_t* block_gates, size_t capacity, size_t* nblocks_out);
+/* attach a trained model (kept by the caller) and the measured time of one pass per register size
+ * (pass_ms[n], milliseconds); NULL detaches */
+int qcs_set_cost_model(qcs_handle h, qcs_mlp_handle mlp, const double* pass_ms, size_t len);
+
 /* ---- engine options ---- */
 enum qcs_option {
 	QCS_OPT_PASSES = 1,          /* 1 (default): gate lists run as shared-memory passes; 0: one kernel per gate */

@@ -104,6 +104,19 @@ SIGNATURES = {
     "qcs_qaoa_batch_amplitudes": (_u64, [_h]),
     "qcs_qaoa_batch_last_error": (C.c_char_p, [_h]),
     "qcs_qaoa_batch_destroy": (_i, [_h]),
+    "qcs_apply_matrix": (_i, [_h, C.POINTER(_u32), _u32, _pd]),
+    "qcs_mlp_create": (_i, [_i, _u64, C.POINTER(_h)]),
+    "qcs_mlp_destroy": (_i, [_h]),
+    "qcs_mlp_num_params": (_i, [_h]),
+    "qcs_mlp_get_params": (_i, [_h, C.POINTER(C.c_float)]),
+    "qcs_mlp_set_params": (_i, [_h, C.POINTER(C.c_float)]),
+    "qcs_mlp_predict": (_i, [_h, C.POINTER(C.c_float), _i, C.POINTER(C.c_float)]),
+    "qcs_mlp_gradient": (_i, [_h, C.POINTER(C.c_float), C.POINTER(C.c_float), _i, C.POINTER(C.c_float),
+                              C.POINTER(C.c_float)]),
+    "qcs_mlp_train": (_i, [_h, C.POINTER(C.c_float), C.POINTER(C.c_float), _i, _i, C.c_float, C.POINTER(C.c_float)]),
+    "qcs_block_features": (_i, [_u32, C.POINTER(_u32), _u32, _u32, C.POINTER(C.c_float)]),
+    "qcs_set_cost_model": (_i, [_h, _h, _pd, _sz]),
+    "qcs_fusion_plan": (_i, [_u32, C.c_void_p, _sz, _i, C.POINTER(C.c_uint64), C.POINTER(_u32), _sz, C.POINTER(_sz)]),
     "qcs_set_option": (_i, [_h, _i, _i]),
     "qcs_profile_enable": (_i, [_h, _i]),
     "qcs_profile_read": (_i, [_h, C.c_void_p, _i, C.POINTER(_i)]),

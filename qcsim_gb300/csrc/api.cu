@@ -186,6 +186,7 @@ void free_register(qcs_handle h) {
 	if (h->sc.h_pinned) cudaFreeHost(h->sc.h_pinned);
 	qcs::batch_release(h);
 	qcs::prof_release(h);
+	qcs::release_cost_model(h);
 	if (h->own_stream && h->stream) cudaStreamDestroy(h->stream);
 	delete h;
 }

@@ -208,6 +208,9 @@ int run_planned(qcs_handle h, const std::vector<PlannedPass>& passes, int kmax, 
 			} else {
 				continue;
 			}
+			if (op.kind == static_cast<uint8_t>(TKind::Dense2) || op.kind == static_cast<uint8_t>(TKind::Dense3) ||
+			    op.kind == static_cast<uint8_t>(TKind::DenseN))
+				tp.dense = 1;
 			std::sort(ins.begin(), ins.end());
 			op.nins = static_cast<uint8_t>(ins.size());
 			for (size_t i = 0; i < ins.size(); ++i) op.ins |= static_cast<uint64_t>(ins[i]) << (8 * i);
@@ -261,20 +264,9 @@ int run_planned(qcs_handle h, const std::vector<PlannedPass>& passes, int kmax, 
 
 }  // namespace
 
-// the fused path: blocks of up to fusion_max qubits, each one dense matrix, applied in shared-memory passes
-int fused_apply(qcs_handle h, const qcs_gate* gates, size_t count) {
+// dense blocks applied in shared-memory passes (the fused path and qcs_apply_matrix)
+int apply_blocks(qcs_handle h, std::vector<FusedBlock> blocks) {
 	const int n = static_cast<int>(h->n);
-	std::vector<CompiledGate> cg;
-	cg.reserve(count);
-	for (size_t i = 0; i < count; ++i) cg.push_back(compile_gate(gates[i], false));
-	FusionPolicy pol;
-	pol.max_qubits = std::min(h->fusion_max, h->prec == QCS_FP64 ? 4 : 5);
-	pol.nqubits = n;
-	if (h->fusion == 2 && h->cost_model) {
-		pol.cost = h->cost_model;
-		pol.ctx = h->cost_ctx;
-	}
-	std::vector<FusedBlock> blocks = fuse(cg, pol);
 	const int kfull = h->prec == QCS_FP64 ? tile_qubits<double>() : tile_qubits<float>();
 	const int kmax = std::min(kfull, n);
 	const int L0 = std::min(n, std::max(5, kmax - 8));
@@ -301,6 +293,28 @@ int fused_apply(qcs_handle h, const qcs_gate* gates, size_t count) {
 	}
 	h->last_blocks = blocks.size();
 	return h->prec == QCS_FP64 ? run_planned<double>(h, passes, kmax, L0) : run_planned<float>(h, passes, kmax, L0);
+}
+
+// the fused path: blocks of up to fusion_max qubits (or the partition the cost model picks)
+int fused_apply(qcs_handle h, const qcs_gate* gates, size_t count) {
+	const int n = static_cast<int>(h->n);
+	std::vector<CompiledGate> cg;
+	cg.reserve(count);
+	for (size_t i = 0; i < count; ++i) cg.push_back(compile_gate(gates[i], false));
+	std::vector<FusedBlock> blocks;
+	if (h->fusion == 2 && h->cost_ctx) {
+		const int kfull = h->prec == QCS_FP64 ? tile_qubits<double>() : tile_qubits<float>();
+		const int kmax = std::min(kfull, n);
+		const int L0 = std::min(n, std::max(5, kmax - 8));
+		const int st = choose_partition(h, cg, kmax, L0, blocks, &h->last_predicted_ms);
+		if (st != QCS_OK) return st;
+	} else {
+		FusionPolicy pol;
+		pol.max_qubits = std::min(h->fusion_max, h->prec == QCS_FP64 ? 4 : 5);
+		pol.nqubits = n;
+		blocks = fuse(cg, pol);
+	}
+	return apply_blocks(h, std::move(blocks));
 }
 
 int batch_apply(qcs_handle h, const qcs_gate* gates, size_t count) {

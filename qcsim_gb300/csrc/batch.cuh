@@ -2,7 +2,10 @@
 // the QFT sequence.
 #pragma once
 
+#include <vector>
+
 #include "engine.cuh"
+#include "fusion.cuh"
 
 namespace qcs {
 
@@ -14,5 +17,12 @@ int batch_apply(qcs_handle h, const qcs_gate* gates, size_t count);
 // QuantumFourierTransform::QFT / IQFT over [start, end]
 int qft_apply(qcs_handle h, uint32_t start, uint32_t end, bool inverse, bool do_swap);
 void batch_release(qcs_handle h);
+
+// dense blocks applied in shared-memory passes
+int apply_blocks(qcs_handle h, std::vector<FusedBlock> blocks);
+// the candidate partition with the lowest predicted time (costmodel.cu)
+int choose_partition(qcs_handle h, const std::vector<CompiledGate>& gates, int kmax, int L0, std::vector<FusedBlock>& best,
+                     double* predicted_ms);
+void release_cost_model(qcs_handle h);
 
 }  // namespace qcs

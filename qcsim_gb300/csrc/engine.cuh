@@ -94,8 +94,8 @@ struct qcs_register {
 	int batch_mode = 1;                    // QCS_OPT_PASSES
 	int fusion = -1;                       // QCS_OPT_FUSION (-1: by precision)
 	int fusion_max = 5;                    // QCS_OPT_FUSION_MAX_QUBITS
-	double (*cost_model)(const std::vector<uint32_t>&, uint32_t, int, void*) = nullptr;  // learned block cost
-	void* cost_ctx = nullptr;
+	void* cost_ctx = nullptr;              // learned partition choice (costmodel.cu)
+	double last_predicted_ms = 0;          // its prediction for the last fused gate list
 	size_t last_blocks = 0;                // blocks of the last fused gate list
 	void* prof = nullptr;                  // launch timing records (profile.cu), when enabled
 	std::string err;

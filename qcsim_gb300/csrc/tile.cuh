@@ -35,6 +35,7 @@ struct TilePass {
 	uint8_t high[32];      // global positions of local bits L..k-1
 	uint8_t fixed[40];     // global positions of the non-tile qubits, ascending
 	uint32_t op_begin, op_count;
+	int dense;             // the pass holds dense-block operations
 };
 
 template <typename T>

@@ -153,7 +153,9 @@ __device__ __forceinline__ void tile_denseN(cplx_t<T>* sm, uint32_t items, const
 	}
 }
 
-template <typename T>
+// DENSE: whether this instantiation carries the dense-block paths (they need many registers; passes
+// without dense blocks run the lighter instantiation at higher occupancy)
+template <typename T, bool DENSE>
 __device__ __forceinline__ void tile_apply(cplx_t<T>* sm, int k, const TileOp& top, const cplx_t<T>* __restrict__ mats, uint64_t base) {
 	const OpRegs op{top.ins, top.nins, top.lset, top.lbit0, top.lbit1, top.lbit2, top.mat};
 	const uint32_t items = (1u << k) >> op.nins;
@@ -202,6 +204,8 @@ __device__ __forceinline__ void tile_apply(cplx_t<T>* sm, int k, const TileOp& t
 				sm[b | op.lbit1] = mk<T>(a.y, -a.x);
 			}
 		}
+	} else if constexpr (!DENSE) {
+		return;
 	} else if (kind == TKind::Dense2) {
 		tile_dense<T, 2>(sm, items, op, mats);
 	} else if (kind == TKind::Dense3) {
@@ -225,7 +229,7 @@ __device__ __forceinline__ void tile_apply(cplx_t<T>* sm, int k, const TileOp& t
 	}
 }
 
-template <typename T>
+template <typename T, bool DENSE>
 __global__ void __launch_bounds__(kTileThreads) k_tile(cplx_t<T>* __restrict__ s, TilePass p, const TileOp* __restrict__ ops,
                                                       const cplx_t<T>* __restrict__ mats, uint64_t ntiles) {
 	extern __shared__ __align__(16) unsigned char smraw[];
@@ -250,7 +254,7 @@ __global__ void __launch_bounds__(kTileThreads) k_tile(cplx_t<T>* __restrict__ s
 		for (uint32_t oi = 0; oi < p.op_count; ++oi) {
 			const TileOp op = ops[p.op_begin + oi];
 			if ((base & op.gmask) != op.gmask) continue;
-			tile_apply<T>(sm, p.k, op, mats, base);
+			tile_apply<T, DENSE>(sm, p.k, op, mats, base);
 			__syncthreads();
 		}
 		for (uint32_t j = threadIdx.x; j < K; j += blockDim.x) s[base | highoff[j >> p.L] | (j & lowmask)] = sm[j];
@@ -268,8 +272,9 @@ cudaError_t launch_tile_pass(cplx_t<T>* s, const TilePass& p, const TileOp* d_op
 	static bool configured = false;
 	const size_t smem = (size_t(1) << p.k) * sizeof(cplx_t<T>);
 	if (!configured) {
-		cudaError_t e = cudaFuncSetAttribute(k_tile<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-		                                     static_cast<int>((size_t(1) << tile_qubits<T>()) * sizeof(cplx_t<T>)));
+		const int maxs = static_cast<int>((size_t(1) << tile_qubits<T>()) * sizeof(cplx_t<T>));
+		cudaError_t e = cudaFuncSetAttribute(k_tile<T, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, maxs);
+		if (e == cudaSuccess) e = cudaFuncSetAttribute(k_tile<T, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, maxs);
 		if (e != cudaSuccess) return e;
 		configured = true;
 	}
@@ -280,7 +285,8 @@ cudaError_t launch_tile_pass(cplx_t<T>* s, const TilePass& p, const TileOp* d_op
 	if (per_sm > 4) per_sm = 4;
 	uint64_t grid = static_cast<uint64_t>(sms) * per_sm;
 	if (grid > ntiles) grid = ntiles;
-	k_tile<T><<<static_cast<unsigned>(grid), kTileThreads, smem, st>>>(s, p, d_ops, d_mats, ntiles);
+	if (p.dense) k_tile<T, true><<<static_cast<unsigned>(grid), kTileThreads, smem, st>>>(s, p, d_ops, d_mats, ntiles);
+	else k_tile<T, false><<<static_cast<unsigned>(grid), kTileThreads, smem, st>>>(s, p, d_ops, d_mats, ntiles);
 	note_launches(1);
 	return cudaGetLastError();
 }

@@ -133,3 +133,32 @@ def test_cpp_dropin_compiles_against_reference_headers():
     r = subprocess.run(cmd, capture_output=True, text=True)
     assert r.returncode == 0, r.stderr[-3000:]
     assert (out / "dropin_check").exists()
+
+
+def test_fusion_plan_covers_every_gate():
+    """the greedy fuser (host code of the engine) keeps every gate, in blocks no wider than asked
+    unless a single gate is wider"""
+    if not L.LIB_PATH.exists():
+        pytest.skip("libqcs_gpu.so not built")
+    from qcsim_gb300 import costmodel
+    for n, mq in ((20, 5), (24, 3), (30, 2), (12, 1)):
+        ops = circuits.layered_circuit(n, 6, seed=n, p3=0.05, controlled_frac=0.1)
+        plan = costmodel.fusion_plan(n, G.records(ops), mq)
+        assert sum(ng for _, ng in plan) == len(ops)
+        for mask, ng in plan:
+            width = bin(mask).count("1")
+            assert width <= max(mq, 3) and ng >= 1
+    # wider blocks never mean more blocks
+    ops = circuits.layered_circuit(26, 8, seed=3)
+    counts = [len(costmodel.fusion_plan(26, G.records(ops), mq)) for mq in (2, 3, 4, 5)]
+    assert counts == sorted(counts, reverse=True)
+
+
+def test_block_features_layout():
+    if not L.LIB_PATH.exists():
+        pytest.skip("libqcs_gpu.so not built")
+    from qcsim_gb300 import costmodel
+    f = costmodel.features(30, (0, 5, 29), 7)
+    assert f.shape == (costmodel.F,)
+    assert f[0] == pytest.approx(3 / 5) and f[1] == pytest.approx(7 / 32) and f[2] == pytest.approx(30 / 32)
+    assert f[5] == pytest.approx(1 / 5) and f[6] == pytest.approx(1 / 5) and f[10] == 1
