@@ -43,7 +43,8 @@ def parse():
     ap.add_argument("--seed", type=int, default=1)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-gates", type=int, default=6, help="gates per CPU step / sample")
-    ap.add_argument("--config", default="layered", choices=["layered", "precision", "qaoa"],
+    ap.add_argument("--model", default=None, help="learned config: cost-model file")
+    ap.add_argument("--config", default="layered", choices=["layered", "precision", "qaoa", "learned"],
                     help="layered: the 30-qubit FP64 circuit (headline); precision: fused FP32 vs plain FP64")
     ap.add_argument("--max-block", type=int, default=5, help="precision config: largest fused block")
     return ap.parse_args()
@@ -495,10 +496,63 @@ def run_qaoa(args):
     print(json.dumps(line))
 
 
+def run_learned(args):
+    """learned fusion on unseen circuits (n qubits, depth, 10% of one-qubit slots controlled rotations):
+    device time and fidelity of the FP32 path with the MLP's partition, with the greedy fuser (largest
+    block 5), and of the unfused plain FP64 path"""
+    import ctypes as C
+    import torch
+    import qcsim_gb300 as Q
+    from qcsim_gb300 import _lib as L, circuits, costmodel, gates as G
+    lib = L.load()
+    n = args.qubits
+    ops = circuits.layered_circuit(n, args.depth, seed=9001 + args.seed, controlled_frac=0.1)
+    recs = G.records(ops)
+    stream = torch.cuda.Stream()
+    mlp, pass_ms = costmodel.load(Path(args.model) if args.model else None)
+
+    def timed(reg):
+        lib.qcs_set_stream(reg.handle, stream.cuda_stream)
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        reg.apply_records(recs)
+        b.record(stream)
+        b.synchronize()
+        return a.elapsed_time(b) / 1e3
+
+    r64 = Q.QubitRegister(n, seed=1)
+    t64 = timed(r64)
+    res = {"fp64_unfused_seconds": t64}
+    for name, setup in (("greedy5", lambda r: r.set_fusion(1, 5)), ("greedy3", lambda r: r.set_fusion(1, 3)),
+                        ("learned", lambda r: costmodel.attach(r, mlp, pass_ms))):
+        r32 = Q.QubitRegister(n, seed=1, precision="fp32")
+        setup(r32)
+        timed(r32)  # the first call includes the partition search and planning
+        r32.setToBasisState(0)
+        t = timed(r32)
+        f, d = C.c_double(), C.c_double()
+        L.check(lib.qcs_compare(r64.handle, r32.handle, C.byref(f), C.byref(d)), r64.handle)
+        res[name] = {"seconds": t, "speedup_vs_fp64": t64 / t, "one_minus_fidelity": 1 - f.value,
+                     "max_abs_amplitude_error": d.value}
+        r32.close()
+    widths = {}
+    for mq in range(1, 6):
+        widths[mq] = len(costmodel.fusion_plan(n, recs, mq))
+    line = {"metric": "learned fusion: MLP partition vs greedy vs unfused FP64", "config": {
+                "workload": f"layered random circuit, {n} qubits, depth {args.depth}, 10% controlled rotations, seed "
+                            f"{9001 + args.seed} (not seen in training)", "gates": len(ops), "blocks_by_max_width": widths},
+            **res, "learned_gain_vs_greedy5": res["greedy5"]["seconds"] / res["learned"]["seconds"], "data": "synthetic"}
+    print(json.dumps(line))
+
+
 def main():
     args = parse()
     if args.config == "precision":
         run_precision(args)
+        return
+    if args.config == "learned":
+        run_learned(args)
         return
     if args.config == "qaoa":
         run_qaoa(args)
