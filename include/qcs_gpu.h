@@ -242,6 +242,21 @@ int qcs_rng_destroy(qcs_rng_handle g);
 /* n uniforms in [0, 1) */
 int qcs_rng_uniform(qcs_rng_handle g, double* out, size_t n);
 
+/* ---- GetQubitProbability without device allocation ----
+ * No reference counterpart: the reference's GetQubitProbability (QubitRegister.h:592-598) sums on
+ * the host, and qcs_qubit_probability above is its replacement.  This variant gives the same value
+ * (to rounding) but reduces through one fixed file-scope device array (256 KiB per GPU, resident
+ * while the library is loaded) instead of scratch the register allocates, for callers that cannot
+ * let the library allocate: a register that fills the GPU, device memory owned by the application's
+ * own pool, or a loop that cannot take the device-wide wait of cudaFree.
+ *  - registers of at most 32 qubits; larger ones return QCS_UNSUPPORTED with a message;
+ *  - call with the register's device current; the first call on a device sets the array up
+ *    (address lookup, kernel loading), so make it before any stream capture on that device;
+ *  - every call uses the same array: calls that can overlap on the GPU (registers on different
+ *    streams, several host threads) race and must be serialised by the caller;
+ *  - nothing needs zeroing first; blocks until the value is on the host. */
+int qcs_qubit_probability_noalloc(qcs_handle h, uint32_t qubit, double* p_out);
+
 #ifdef __cplusplus
 }
 #endif

@@ -124,6 +124,7 @@ SIGNATURES = {
     "qcs_rng_create": (_i, [_u64, C.POINTER(_h)]),
     "qcs_rng_destroy": (_i, [_h]),
     "qcs_rng_uniform": (_i, [_h, _pd, _sz]),
+    "qcs_qubit_probability_noalloc": (_i, [_h, _u32, _pd]),
 }
 
 

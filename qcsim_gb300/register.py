@@ -212,6 +212,13 @@ class QubitRegister:
         self._ck(self._lib.qcs_qubit_probability(self._h, qubit, C.byref(out)))
         return out.value
 
+    def GetQubitProbabilityNoAlloc(self, qubit: int) -> float:
+        """GetQubitProbability through the library's fixed device array (qcs_qubit_probability_noalloc):
+        no device allocation, registers of at most 32 qubits, calls must not overlap on the GPU."""
+        out = C.c_double()
+        self._ck(self._lib.qcs_qubit_probability_noalloc(self._h, qubit, C.byref(out)))
+        return out.value
+
     def probabilities(self) -> np.ndarray:
         out = np.empty(self.NrBasisStates, dtype=np.float64)
         self._ck(self._lib.qcs_probabilities(self._h, L.dptr(out)))
