@@ -288,7 +288,7 @@ def run_gb300(args):
     value = gates * world / (ms_max / 1e3)
     peak, peak_kind = peaks()
     hbm_frac = alg_bytes / (ms / 1e3) / (peak * 1e9)
-    roofline = roofline_of(prof, peak, peak_kind)
+    roofline = roofline_of(prof, peak, peak_kind, n, alg_bytes)
 
     # end to end through the C ABI: host gate records in, a qubit probability out, every step
     barrier(dist)
@@ -363,34 +363,39 @@ def run_gb300(args):
         dist.destroy_process_group()
 
 
-def roofline_of(prof: dict, peak: float, peak_kind: str) -> dict:
-    """the kernel family with the largest share of device time: algorithmic bytes per launch over its
-    average launch duration"""
+def roofline_of(prof: dict, peak: float, peak_kind: str, n: int, gate_bytes: float) -> dict:
+    """the kernel family with the largest share of device time, as an HBM roofline point.
+
+    achieved = algorithmic bytes per launch / average launch duration, where the algorithmic bytes are
+    the per-gate figure 2 x 16 B x 2^n x f(g) summed over the gates the launches applied (f = fraction of
+    rows of the gate matrix that differ from the identity).  When the family ran every launch of the
+    timed region (the shared-memory pass does on the layered circuit), those are all the gates timed.
+    pass_bytes_per_launch is what one launch must move at least (every amplitude it touches read and
+    written once); traffic is the DRAM bytes ncu measured for one launch of the family."""
     total = sum(v[1] for v in prof.values()) or 1.0
+    all_launches = sum(v[0] for v in prof.values())
     dom = max(prof, key=lambda k: prof[k][1])
-    launches, ms, nbytes = prof[dom]
-    achieved = nbytes / (ms / 1e3) / 1e9
+    launches, ms, pass_bytes = prof[dom]
+    alg_per_launch = gate_bytes / launches if launches == all_launches else pass_bytes / launches
+    avg_s = ms / launches / 1e3
+    achieved = alg_per_launch / avg_s / 1e9
     return {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-            "traffic": read_traffic(dom), "kernel": dom, "peak_source": peak_kind,
-            "algorithmic_bytes_per_launch": nbytes / launches, "avg_launch_ms": ms / launches,
+            "traffic": read_traffic(dom, n), "kernel": dom, "peak_source": peak_kind,
+            "algorithmic_bytes_per_launch": alg_per_launch, "avg_launch_ms": ms / launches,
+            "pass_bytes_per_launch": pass_bytes / launches, "pass_GBps": pass_bytes / launches / avg_s / 1e9,
             "share_of_device_time": ms / total, "launches": launches}
 
 
-def family(gate) -> str:
-    name = type(gate).__name__
-    return {"HadamardGate": "ctrl1q_real", "RyGate": "ctrl1q_real", "RxGate": "ctrl1q_rxlike", "RzGate": "ctrl1q_diag",
-            "CNOTGate": "ctrl1q_swap", "ToffoliGate": "ctrl1q_swap_cc", "CCZGate": "ctrl1q_phaseneg_cc"}.get(name, name)
-
-
-def read_traffic(kernel_family: str):
-    """DRAM bytes per launch from the committed ncu summary (profiles/*.md, a line
-    'traffic <family> <bytes>'), or None"""
+def read_traffic(kernel_family: str, n: int):
+    """DRAM bytes per launch from the committed ncu summaries (profiles/*.md, a line
+    'traffic <family> <bytes> qubits <m>'), scaled by 2^(n - m): a launch of these families sweeps the
+    whole register, so its traffic grows in proportion to the amplitude count.  None if not captured."""
     for p in sorted((ROOT / "profiles").glob("*.md")):
         for ln in p.read_text().splitlines():
             parts = ln.strip().strip("|").split()
-            if len(parts) >= 3 and parts[0] == "traffic" and parts[1] == kernel_family:
+            if len(parts) >= 5 and parts[0] == "traffic" and parts[1] == kernel_family and parts[3] == "qubits":
                 try:
-                    return float(parts[2])
+                    return float(parts[2]) * 2.0 ** (n - int(parts[4]))
                 except ValueError:
                     pass
     return None
