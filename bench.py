@@ -42,7 +42,7 @@ def parse():
     ap.add_argument("--depth", type=int, default=60)
     ap.add_argument("--seed", type=int, default=1)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--cpu-gates", type=int, default=6, help="gates per CPU step / sample")
+    ap.add_argument("--cpu-gates", type=int, default=60, help="gates in the CPU baseline sample (a third per reference-arm step)")
     ap.add_argument("--model", default=None, help="learned config: cost-model file")
     ap.add_argument("--config", default="layered", choices=["layered", "precision", "qaoa", "learned"],
                     help="layered: the 30-qubit FP64 circuit (headline); precision: fused FP32 vs plain FP64")
