@@ -79,6 +79,13 @@ cudaError_t ensure(void** p, size_t* cap, size_t bytes) {
 	return e;
 }
 
+template <typename T> cplx_t<T> mk_host(double re, double im) {
+	cplx_t<T> c;
+	c.x = static_cast<T>(re);
+	c.y = static_cast<T>(im);
+	return c;
+}
+
 template <typename T> void push_mat2(std::vector<cplx_t<T>>& mats, const Mat2<double>& m) {
 	const double2 v[4] = {m.m00, m.m01, m.m10, m.m11};
 	for (const double2& x : v) {
@@ -102,6 +109,13 @@ bool op_in_bounds(const TileOp& op, int k, size_t mats) {
 		insmask |= 1u << b;
 	}
 	if ((op.lset & ~insmask) != 0) return false;
+	if (static_cast<TKind>(op.kind) == TKind::PhaseRow) {
+		// lbit1 / lbit2 hold the row's first bit and width; the table covers every z = y << shift
+		const uint32_t shift = op.pad[0], S = op.pad[1], M = op.pad[3];
+		if (op.nins > 1 || op.lbit0 != 0 || M < 1 || M > 40 || S > M || op.lbit1 + op.lbit2 > 64 || op.lbit2 + shift > M)
+			return false;
+		return op.mat + (size_t(1) << (M - S)) + (size_t(1) << S) <= mats;
+	}
 	const bool flag0 = static_cast<TKind>(op.kind) == TKind::GlobalDiag;  // lbit0 is a side flag there
 	for (uint32_t bit : {flag0 ? 0u : op.lbit0, op.lbit1, op.lbit2})
 		if ((bit & ~insmask) != 0 || (bit & (bit - 1)) != 0) return false;
@@ -123,6 +137,24 @@ int run_planned(qcs_handle h, const std::vector<PlannedPass>& passes, int kmax, 
 	std::vector<TilePass> tps;
 	std::vector<TileOp> ops;
 	std::vector<cplx_t<T>> mats;
+	// QFT phase rows share one pair of tables of 2^M-th roots of unity: hi[u] = w^(u 2^S), lo[v] = w^v
+	uint32_t rowM = 0, rowS = 0, row_tab = 0;
+	for (const PlannedPass& pp : passes)
+		for (const CompiledGate& c : pp.gates)
+			if (c.kind == GKind::PhaseRow) rowM = std::max(rowM, c.row_bits + 1);
+	if (rowM > 0) {
+		rowS = (rowM + 1) / 2;
+		row_tab = static_cast<uint32_t>(mats.size());
+		const double two_pi = 2.0 * M_PI;
+		for (uint64_t u = 0; u < (1ULL << (rowM - rowS)); ++u) {
+			const double a = two_pi * std::ldexp(static_cast<double>(u), static_cast<int>(rowS) - static_cast<int>(rowM));
+			mats.push_back(mk_host<T>(std::cos(a), std::sin(a)));
+		}
+		for (uint64_t v = 0; v < (1ULL << rowS); ++v) {
+			const double a = two_pi * std::ldexp(static_cast<double>(v), -static_cast<int>(rowM));
+			mats.push_back(mk_host<T>(std::cos(a), std::sin(a)));
+		}
+	}
 	for (const PlannedPass& pp : passes) {
 		// tile qubits: the required ones, completed from the bottom up to kmax
 		uint64_t T_ = pp.tmask | ((1ULL << L0) - 1);
@@ -196,6 +228,21 @@ int run_planned(qcs_handle h, const std::vector<PlannedPass>& passes, int kmax, 
 					v.y = static_cast<T>(c.dense_m[2 * i + 1]);
 					mats.push_back(v);
 				}
+			} else if (c.kind == GKind::PhaseRow) {
+				op.kind = static_cast<uint8_t>(TKind::PhaseRow);
+				if ((T_ >> c.target) & 1ULL) {
+					op.lset |= 1u << lpos[c.target];
+					ins.push_back(lpos[c.target]);
+				} else {
+					op.gmask |= 1ULL << c.target;
+				}
+				op.lbit1 = c.row_lo;
+				op.lbit2 = c.row_bits;
+				op.pad[0] = static_cast<uint8_t>(rowM - 1 - c.row_bits);
+				op.pad[1] = static_cast<uint8_t>(rowS);
+				op.pad[2] = c.row_inverse ? 1 : 0;
+				op.pad[3] = static_cast<uint8_t>(rowM);
+				op.mat = row_tab;
 			} else if (c.kind == GKind::Block) {
 				op.kind = static_cast<uint8_t>(TKind::DenseN);
 				for (uint32_t q : c.block_q) ins.push_back(lpos[q]);
@@ -317,26 +364,14 @@ int fused_apply(qcs_handle h, const qcs_gate* gates, size_t count) {
 	return apply_blocks(h, std::move(blocks));
 }
 
-int batch_apply(qcs_handle h, const qcs_gate* gates, size_t count) {
-	const int n = static_cast<int>(h->n);
-	const int fusion = h->fusion >= 0 ? h->fusion : (h->prec == QCS_FP32 ? 1 : 0);
-	if (fusion > 0 && count > 0) return fused_apply(h, gates, count);
-	const int kmax = h->prec == QCS_FP64 ? tile_qubits<double>() : tile_qubits<float>();
-	if (n < kmax + 2 || count < 2 || h->batch_mode == 0) {
-		for (size_t i = 0; i < count; ++i) {
-			cudaError_t e = apply_one(h, gates[i]);
-			if (e != cudaSuccess) {
-				h->err = std::string("apply gates: ") + cudaGetErrorString(e);
-				return QCS_CUDA_ERROR;
-			}
-		}
-		return QCS_OK;
-	}
+namespace {
+
+// packs compiled gates into shared-memory passes (greedy, in order) and runs them
+int plan_and_run(qcs_handle h, const std::vector<CompiledGate>& cg, int kmax) {
 	const int L0 = std::max(5, kmax - 8);
 	std::vector<PlannedPass> passes(1);
 	passes.back().tmask = (1ULL << L0) - 1;
-	for (size_t i = 0; i < count; ++i) {
-		CompiledGate c = compile_gate(gates[i], true);
+	for (const CompiledGate& c : cg) {
 		h->scale *= c.scale;
 		const double mag = std::abs(h->scale);
 		if (c.kind != GKind::Identity) {
@@ -358,6 +393,34 @@ int batch_apply(qcs_handle h, const qcs_gate* gates, size_t count) {
 		}
 	}
 	return h->prec == QCS_FP64 ? run_planned<double>(h, passes, kmax, L0) : run_planned<float>(h, passes, kmax, L0);
+}
+
+// whether a gate list on this register runs one kernel per gate (small registers, short lists, or
+// passes switched off)
+bool per_gate_mode(qcs_handle h, size_t count, int kmax) {
+	return static_cast<int>(h->n) < kmax + 2 || count < 2 || h->batch_mode == 0;
+}
+
+}  // namespace
+
+int batch_apply(qcs_handle h, const qcs_gate* gates, size_t count) {
+	const int fusion = h->fusion >= 0 ? h->fusion : (h->prec == QCS_FP32 ? 1 : 0);
+	if (fusion > 0 && count > 0) return fused_apply(h, gates, count);
+	const int kmax = h->prec == QCS_FP64 ? tile_qubits<double>() : tile_qubits<float>();
+	if (per_gate_mode(h, count, kmax)) {
+		for (size_t i = 0; i < count; ++i) {
+			cudaError_t e = apply_one(h, gates[i]);
+			if (e != cudaSuccess) {
+				h->err = std::string("apply gates: ") + cudaGetErrorString(e);
+				return QCS_CUDA_ERROR;
+			}
+		}
+		return QCS_OK;
+	}
+	std::vector<CompiledGate> cg;
+	cg.reserve(count);
+	for (size_t i = 0; i < count; ++i) cg.push_back(compile_gate(gates[i], true));
+	return plan_and_run(h, cg, kmax);
 }
 
 std::vector<qcs_gate> qft_gates(uint32_t start, uint32_t end, bool inverse, bool do_swap) {
@@ -393,9 +456,65 @@ std::vector<qcs_gate> qft_gates(uint32_t start, uint32_t end, bool inverse, bool
 	return gs;
 }
 
+namespace {
+
+// QFT rows narrower than this stay individual controlled phases (a row costs two complex products on
+// half the amplitudes; a controlled phase one product on a quarter)
+constexpr uint32_t kMinRowBits = 5;
+
+// the QFT's gate sequence with each target's run of controlled phases as one PhaseRow: the phases
+// commute (all diagonal) and sit between the same two Hadamards, so their product is applied at once
+std::vector<CompiledGate> qft_compiled(uint32_t start, uint32_t end, bool inverse, bool do_swap) {
+	std::vector<CompiledGate> cg;
+	const int sq = static_cast<int>(start), eq = static_cast<int>(end);
+	auto swaps = [&]() {
+		uint32_t a = start, b = end;
+		while (a < b) cg.push_back(compile_gate(make_swap(a++, b--), true));
+	};
+	auto row = [&](int cur) {
+		const uint32_t bits = static_cast<uint32_t>(cur - sq);
+		if (bits >= kMinRowBits) {
+			CompiledGate c;
+			c.kind = GKind::PhaseRow;
+			c.target = static_cast<uint32_t>(cur);
+			c.row_lo = start;
+			c.row_bits = bits;
+			c.row_inverse = inverse;
+			cg.push_back(c);
+			return;
+		}
+		double phase = inverse ? -M_PI_2 : M_PI_2;
+		for (int c = cur - 1; c >= sq; --c) {
+			cg.push_back(compile_gate(make_cp(cur, c, phase), true));
+			phase *= 0.5;
+		}
+	};
+	if (!inverse) {
+		cg.push_back(compile_gate(make_h(eq), true));
+		for (int cur = eq; cur > sq; --cur) {
+			row(cur);
+			cg.push_back(compile_gate(make_h(cur - 1), true));
+		}
+		if (do_swap) swaps();
+	} else {
+		if (do_swap) swaps();
+		for (int cur = sq + 1; cur <= eq; ++cur) {
+			cg.push_back(compile_gate(make_h(cur - 1), true));
+			row(cur);
+		}
+		cg.push_back(compile_gate(make_h(eq), true));
+	}
+	return cg;
+}
+
+}  // namespace
+
 int qft_apply(qcs_handle h, uint32_t start, uint32_t end, bool inverse, bool do_swap) {
 	const std::vector<qcs_gate> gs = qft_gates(start, end, inverse, do_swap);
-	return batch_apply(h, gs.data(), gs.size());
+	const int fusion = h->fusion >= 0 ? h->fusion : (h->prec == QCS_FP32 ? 1 : 0);
+	const int kmax = h->prec == QCS_FP64 ? tile_qubits<double>() : tile_qubits<float>();
+	if (fusion > 0 || per_gate_mode(h, gs.size(), kmax)) return batch_apply(h, gs.data(), gs.size());
+	return plan_and_run(h, qft_compiled(start, end, inverse, do_swap), kmax);
 }
 
 void batch_release(qcs_handle h) {

@@ -127,6 +127,7 @@ const char* kernel_name(const CompiledGate& c) {
 	case GKind::Swap: return c.ncontrols ? "swap_controlled" : "swap";
 	case GKind::Dense: return c.dense_k == 2 ? "dense2" : "dense3";
 	case GKind::Block: return "block";
+	case GKind::PhaseRow: return "phase_row";
 	default: return "identity";
 	}
 }
@@ -140,6 +141,7 @@ double touched_fraction(const CompiledGate& c) {
 	case GKind::Swap: return ctl * 0.5;
 	case GKind::Dense: return ctl;
 	case GKind::Block: return 1.0;
+	case GKind::PhaseRow: return 0.5;
 	default: return 0.0;
 	}
 }
@@ -167,6 +169,7 @@ uint64_t CompiledGate::local_mask() const {
 uint64_t CompiledGate::touch_mask() const {
 	uint64_t m = local_mask();
 	if (kind == GKind::Ctrl1q) m |= 1ULL << target;
+	if (kind == GKind::PhaseRow) m |= (1ULL << target) | (((1ULL << row_bits) - 1) << row_lo);
 	for (uint32_t i = 0; i < ncontrols; ++i) m |= 1ULL << controls[i];
 	return m;
 }
@@ -290,6 +293,8 @@ template <typename T> cudaError_t launch_compiled(cplx_t<T>* s, uint64_t N, cons
 		std::memcpy(a.m, c.dense_m, sizeof(a.m));
 		return launch_dense<T>(s, N, a, plan_for(ins, set), sms, st);
 	}
+	case GKind::Block:
+	case GKind::PhaseRow: break;  // shared-memory passes only
 	}
 	return cudaErrorInvalidValue;
 }

@@ -15,7 +15,8 @@ enum class GKind : int {
 	Ctrl1q,        // 2x2 block on `target`, under `controls`
 	Swap,          // exchange base|bitA with base|bitB, under `controls`
 	Dense,         // 4x4 or 8x8 block on dense_q, under `controls`
-	Block          // fused block: dense 2^m x 2^m matrix on block_q (ascending), no controls
+	Block,         // fused block: dense 2^m x 2^m matrix on block_q (ascending), no controls
+	PhaseRow       // the QFT's run of controlled phases on one target (see below); shared-memory passes only
 };
 
 struct CompiledGate {
@@ -30,11 +31,16 @@ struct CompiledGate {
 	uint32_t qa = 0, qb = 0;    // Swap: exchange |..qa=1..qb=0..> with |..qa=0..qb=1..>
 	int dense_k = 0;
 	uint32_t dense_q[3] = {0, 0, 0};  // qubit of matrix bit 0, 1, 2
-	double dense_m[128];
+	double dense_m[128] = {};
 	std::complex<double> scale{1.0, 0.0};  // global factor taken out of the matrix
 	std::vector<uint32_t> block_q;          // Block: qubits, ascending (matrix bit j <-> block_q[j])
 	std::vector<std::complex<double>> block_m;  // Block: row-major 2^m x 2^m
 	uint32_t block_gates = 0;               // Block: original gates folded in
+	// PhaseRow: amplitudes with bit `target` set get exp(+-2 pi i y / 2^(row_bits + 1)), y = the integer
+	// in bits row_lo .. row_lo + row_bits - 1: the product of ControlledPhaseShift(pi / 2^(target - c))
+	// over controls c = target - 1 .. row_lo, the phases one QFT step applies to one target
+	uint32_t row_lo = 0, row_bits = 0;
+	bool row_inverse = false;
 
 	// qubits whose bit a tile must hold locally to apply this gate (targets of non-diagonal blocks)
 	uint64_t local_mask() const;

@@ -9,7 +9,10 @@
 namespace qcs {
 
 // DenseN: a fused block's 2^nins x 2^nins matrix whose bit j is the j-th inserted position
-enum class TKind : uint8_t { Ctrl1q = 0, Swap = 1, Dense2 = 2, Dense3 = 3, GlobalDiag = 4, DenseN = 5 };
+// PhaseRow: a QFT phase row (CompiledGate::PhaseRow): lbit1 = row_lo, lbit2 = row_bits, pad[0] = the
+// shift taking y to the table's 2^M-th roots, pad[1] = S, pad[2] = inverse, pad[3] = M; the factor
+// exp(2 pi i z / 2^M), z = y << shift, is table[mat + (z >> S)] * table[mat + 2^(M-S) + (z & (2^S - 1))]
+enum class TKind : uint8_t { Ctrl1q = 0, Swap = 1, Dense2 = 2, Dense3 = 3, GlobalDiag = 4, DenseN = 5, PhaseRow = 6 };
 
 // one gate inside a pass, in tile-local bit positions
 struct TileOp {

@@ -153,10 +153,34 @@ __device__ __forceinline__ void tile_denseN(cplx_t<T>* sm, uint32_t items, const
 	}
 }
 
+// QFT phase row: amplitudes with the target bit set (forced through lset when the target is a tile
+// qubit, selected through gmask otherwise) are multiplied by exp(+-2 pi i y / 2^m), y read from the
+// amplitude's global index; the root comes from two tables (high and low bits of z = y << shift)
+template <typename T>
+__device__ __forceinline__ void tile_phaserow(cplx_t<T>* sm, uint32_t items, const OpRegs op, const TileOp& top,
+                                              const cplx_t<T>* __restrict__ mats, uint64_t base, const uint64_t* highoff, int L) {
+	const uint32_t row_lo = op.lbit1, row_bits = op.lbit2;
+	const uint32_t shift = top.pad[0], S = top.pad[1], M = top.pad[3];
+	const bool inverse = top.pad[2] != 0;
+	const uint64_t ymask = (1ULL << row_bits) - 1, smask = (1ULL << S) - 1;
+	const cplx_t<T>* hi = mats + op.mat;
+	const cplx_t<T>* lo = hi + (1ULL << (M - S));
+	const uint32_t lowmask = (1u << L) - 1;
+	for (uint32_t i = threadIdx.x; i < items; i += blockDim.x) {
+		const uint32_t b = expand_local(i, op);
+		const uint64_t g = base | highoff[b >> L] | (b & lowmask);
+		const uint64_t z = ((g >> row_lo) & ymask) << shift;
+		cplx_t<T> w = cmul<T>(hi[z >> S], lo[z & smask]);
+		if (inverse) w.y = -w.y;
+		sm[b] = cmul<T>(sm[b], w);
+	}
+}
+
 // DENSE: whether this instantiation carries the dense-block paths (they need many registers; passes
 // without dense blocks run the lighter instantiation at higher occupancy)
 template <typename T, bool DENSE>
-__device__ __forceinline__ void tile_apply(cplx_t<T>* sm, int k, const TileOp& top, const cplx_t<T>* __restrict__ mats, uint64_t base) {
+__device__ __forceinline__ void tile_apply(cplx_t<T>* sm, int k, const TileOp& top, const cplx_t<T>* __restrict__ mats, uint64_t base,
+                                           const uint64_t* highoff, int L) {
 	const OpRegs op{top.ins, top.nins, top.lset, top.lbit0, top.lbit1, top.lbit2, top.mat};
 	const uint32_t items = (1u << k) >> op.nins;
 	const TKind kind = static_cast<TKind>(top.kind);
@@ -204,6 +228,8 @@ __device__ __forceinline__ void tile_apply(cplx_t<T>* sm, int k, const TileOp& t
 				sm[b | op.lbit1] = mk<T>(a.y, -a.x);
 			}
 		}
+	} else if (kind == TKind::PhaseRow) {
+		tile_phaserow<T>(sm, items, op, top, mats, base, highoff, L);
 	} else if constexpr (!DENSE) {
 		return;
 	} else if (kind == TKind::Dense2) {
@@ -254,7 +280,7 @@ __global__ void __launch_bounds__(kTileThreads) k_tile(cplx_t<T>* __restrict__ s
 		for (uint32_t oi = 0; oi < p.op_count; ++oi) {
 			const TileOp op = ops[p.op_begin + oi];
 			if ((base & op.gmask) != op.gmask) continue;
-			tile_apply<T, DENSE>(sm, p.k, op, mats, base);
+			tile_apply<T, DENSE>(sm, p.k, op, mats, base, highoff, p.L);
 			__syncthreads();
 		}
 		for (uint32_t j = threadIdx.x; j < K; j += blockDim.x) s[base | highoff[j >> p.L] | (j & lowmask)] = sm[j];

@@ -367,6 +367,23 @@ def test_qft_passes(Q):
     assert np.abs(got - oracle_state(n, circuits.qft_circuit(0, n - 1), v)).max() <= TOL
 
 
+@pytest.mark.parametrize("start,end", [(0, 17), (2, 15), (1, 17), (0, 8), (9, 17)])
+def test_qft_phase_rows(Q, start, end):
+    """QFT / IQFT on a sub-register of an 18-qubit register (shared-memory passes, each target's run of
+    controlled phases applied as one row) against the oracle's gate-by-gate sequence"""
+    from qcsim_gb300 import algorithms, circuits
+    n = 18
+    v = circuits.random_normal_state(n, 21 + start + end)
+    for inverse in (False, True):
+        for do_swap in (False, True):
+            reg = Q.QubitRegister(n, seed=1)
+            reg.setRegisterStorageFastNoNormalize(v)
+            qft = algorithms.QuantumFourierTransform(n, start, end)
+            (qft.IQFT if inverse else qft.QFT)(reg, do_swap)
+            want = oracle_state(n, circuits.qft_circuit(start, end, inverse=inverse, do_swap=do_swap), v)
+            assert np.abs(reg.getRegisterStorage() - want).max() <= TOL, (inverse, do_swap)
+
+
 @pytest.mark.parametrize("n,max_q", [(10, 5), (16, 5), (18, 3), (20, 4)])
 def test_fused_fp32(Q, n, max_q):
     """the FP32 fused path (blocks of <= max_q qubits, one dense matrix each) against the FP64 oracle:
