@@ -20,6 +20,7 @@ QCS_FP64, QCS_FP32 = 0, 1
 QCS_OPT_PASSES = 1
 QCS_OPT_FUSION = 2
 QCS_OPT_FUSION_MAX_QUBITS = 3
+QCS_OPT_TENSOR_CORES = 4
 
 TRAIT_DIAGONAL = 1
 TRAIT_ANTIDIAGONAL = 2

@@ -304,6 +304,10 @@ int qcs_set_option(qcs_handle h, int option, int value) {
 		h->fusion_max = value;
 		return QCS_OK;
 	}
+	if (option == QCS_OPT_TENSOR_CORES) {
+		h->tensor_cores = value ? 1 : 0;
+		return QCS_OK;
+	}
 	return fail(h, QCS_INVALID_ARGUMENT, "unknown option");
 }
 

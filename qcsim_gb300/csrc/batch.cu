@@ -13,6 +13,7 @@
 #include "batch.cuh"
 #include "compile.cuh"
 #include "fusion.cuh"
+#include "tcgen05.cuh"
 #include "tile.cuh"
 
 namespace qcs {
@@ -67,6 +68,7 @@ struct BatchBuffers {
 	size_t ops_cap = 0;
 	void* d_mats = nullptr;
 	size_t mats_cap = 0;
+	int* d_err = nullptr;  // status word of the tensor-core passes
 };
 
 cudaError_t ensure(void** p, size_t* cap, size_t bytes) {
@@ -96,6 +98,39 @@ template <typename T> void push_mat2(std::vector<cplx_t<T>>& mats, const Mat2<do
 	}
 }
 
+// round to TF32 (10 mantissa bits), to nearest with ties away from zero, as cvt.rna.tf32.f32
+float tf32_rna_host(float x) {
+	uint32_t u;
+	std::memcpy(&u, &x, 4);
+	u = (u + 0x1000u) & 0xFFFFE000u;
+	float r;
+	std::memcpy(&r, &u, 4);
+	return r;
+}
+
+// a fused block's real-expanded matrix B (2D x 2D, B[2j + p][2i + q]; see the tensor-core pass kernel)
+// as the MMA's B operand: rows = outputs 2i + q, K = inputs 2j + p, K-major; TF32 hi split then lo
+void push_block_tc(std::vector<float2>& mats, const std::vector<std::complex<double>>& M, uint32_t D) {
+	const uint32_t kdim = 2 * D, split = 4 * D * D;  // floats per split (16 D^2 bytes)
+	if (mats.size() & 1) mats.push_back(make_float2(0.f, 0.f));  // 16-byte alignment of the block
+	std::vector<float> f(2 * split, 0.f);
+	for (uint32_t i = 0; i < D; ++i)
+		for (uint32_t j = 0; j < D; ++j) {
+			const double re = M[static_cast<size_t>(i) * D + j].real(), im = M[static_cast<size_t>(i) * D + j].imag();
+			const double e[2][2] = {{re, im}, {-im, re}};  // [p][q]: input part p -> output part q
+			for (uint32_t pi = 0; pi < 2; ++pi)
+				for (uint32_t qo = 0; qo < 2; ++qo) {
+					const double x = e[pi][qo];
+					const float hi = tf32_rna_host(static_cast<float>(x));
+					const float lo = tf32_rna_host(static_cast<float>(x - static_cast<double>(hi)));
+					const uint32_t off = tc::kmajor_offset(2 * i + qo, 2 * j + pi, kdim) / 4;
+					f[off] = hi;
+					f[split + off] = lo;
+				}
+		}
+	for (size_t k = 0; k < f.size(); k += 2) mats.push_back(make_float2(f[k], f[k + 1]));
+}
+
 // host check of one tile operation: inserted positions strictly ascending and below k, the bits it
 // reads or forces inside the inserted set, its matrix entries inside the table
 bool op_in_bounds(const TileOp& op, int k, size_t mats) {
@@ -109,6 +144,13 @@ bool op_in_bounds(const TileOp& op, int k, size_t mats) {
 		insmask |= 1u << b;
 	}
 	if ((op.lset & ~insmask) != 0) return false;
+	if (static_cast<TKind>(op.kind) == TKind::DenseTC) {
+		const uint32_t D = 1u << op.nins;
+		if (k != kTcTileQubits || op.nins < 4 || op.nins > 5 || op.lset != 0 || op.lbit0 != 0 || op.lbit2 != 0 || (op.mat & 1u) ||
+		    (op.lbit1 & 15u) || op.lbit1 + 32 * D * D > kTcMatBudget)
+			return false;
+		return op.mat + size_t(4) * D * D <= mats;
+	}
 	if (static_cast<TKind>(op.kind) == TKind::PhaseRow) {
 		// lbit1 / lbit2 hold the row's first bit and width; the table covers every z = y << shift
 		const uint32_t shift = op.pad[0], S = op.pad[1], M = op.pad[3];
@@ -180,6 +222,8 @@ int run_planned(qcs_handle h, const std::vector<PlannedPass>& passes, int kmax, 
 			if (!((T_ >> q) & 1ULL)) tp.fixed[nf++] = static_cast<uint8_t>(q);
 		tp.nfixed = nf;
 		tp.op_begin = static_cast<uint32_t>(ops.size());
+		uint32_t tc_slot = 0;  // bytes of resident block matrices used in this pass
+		const bool tc_pass = sizeof(T) == 4 && h->tensor_cores && tp.k == kTcTileQubits && L >= 5 && tp.k - L <= 8;
 		for (const CompiledGate& c : pp.gates) {
 			TileOp op;
 			std::memset(&op, 0, sizeof(op));
@@ -243,6 +287,18 @@ int run_planned(qcs_handle h, const std::vector<PlannedPass>& passes, int kmax, 
 				op.pad[2] = c.row_inverse ? 1 : 0;
 				op.pad[3] = static_cast<uint8_t>(rowM);
 				op.mat = row_tab;
+			} else if (c.kind == GKind::Block && tc_pass && c.block_q.size() >= 4 &&
+			           tc_slot + 32u * (1u << (2 * c.block_q.size())) <= kTcMatBudget) {
+				if constexpr (sizeof(T) == 4) {
+					op.kind = static_cast<uint8_t>(TKind::DenseTC);
+					for (uint32_t q : c.block_q) ins.push_back(lpos[q]);
+					if (mats.size() & 1) mats.push_back(mk_host<T>(0.0, 0.0));
+					op.mat = static_cast<uint32_t>(mats.size());
+					push_block_tc(mats, c.block_m, 1u << c.block_q.size());
+					op.lbit1 = tc_slot;
+					tc_slot += 32u * (1u << (2 * c.block_q.size()));
+					tp.dense = 2;
+				}
 			} else if (c.kind == GKind::Block) {
 				op.kind = static_cast<uint8_t>(TKind::DenseN);
 				for (uint32_t q : c.block_q) ins.push_back(lpos[q]);
@@ -255,8 +311,8 @@ int run_planned(qcs_handle h, const std::vector<PlannedPass>& passes, int kmax, 
 			} else {
 				continue;
 			}
-			if (op.kind == static_cast<uint8_t>(TKind::Dense2) || op.kind == static_cast<uint8_t>(TKind::Dense3) ||
-			    op.kind == static_cast<uint8_t>(TKind::DenseN))
+			if ((op.kind == static_cast<uint8_t>(TKind::Dense2) || op.kind == static_cast<uint8_t>(TKind::Dense3) ||
+			     op.kind == static_cast<uint8_t>(TKind::DenseN)) && tp.dense == 0)
 				tp.dense = 1;
 			std::sort(ins.begin(), ins.end());
 			op.nins = static_cast<uint8_t>(ins.size());
@@ -289,11 +345,16 @@ int run_planned(qcs_handle h, const std::vector<PlannedPass>& passes, int kmax, 
 		e = cudaMemcpyAsync(bb->d_ops, ops.data(), ops.size() * sizeof(TileOp), cudaMemcpyHostToDevice, h->stream);
 	if (e == cudaSuccess && !mats.empty())
 		e = cudaMemcpyAsync(bb->d_mats, mats.data(), mats.size() * sizeof(cplx_t<T>), cudaMemcpyHostToDevice, h->stream);
+	bool any_tc = false;
+	for (const TilePass& tp : tps) any_tc = any_tc || tp.dense == 2;
+	if (e == cudaSuccess && any_tc && !bb->d_err) e = cudaMalloc(&bb->d_err, sizeof(int));
+	if (e == cudaSuccess && any_tc) e = cudaMemsetAsync(bb->d_err, 0, sizeof(int), h->stream);
 	auto* s = static_cast<cplx_t<T>*>(h->d_state);
 	for (size_t i = 0; i < tps.size() && e == cudaSuccess; ++i) {
 		if (tps[i].op_count > 0) {
-			prof_begin(h, "tile_pass", 2.0 * sizeof(cplx_t<T>) * static_cast<double>(h->N));
-			e = launch_tile_pass<T>(s, tps[i], static_cast<const TileOp*>(bb->d_ops), static_cast<const cplx_t<T>*>(bb->d_mats), h->sms, h->stream);
+			prof_begin(h, tps[i].dense == 2 ? "tile_pass_tc" : "tile_pass", 2.0 * sizeof(cplx_t<T>) * static_cast<double>(h->N));
+			e = launch_tile_pass<T>(s, tps[i], static_cast<const TileOp*>(bb->d_ops), static_cast<const cplx_t<T>*>(bb->d_mats), h->sms,
+			                        h->stream, bb->d_err);
 			prof_end(h);
 		}
 		const std::complex<double> f = passes[i].fold_after;
@@ -301,9 +362,16 @@ int run_planned(qcs_handle h, const std::vector<PlannedPass>& passes, int kmax, 
 			e = launch_scale_complex<T>(s, h->N, f.real(), f.imag(), h->sms, h->stream);
 	}
 	// the host vectors must outlive the (pageable, stream-ordered) copies
+	int tc_status = 0;
+	if (e == cudaSuccess && any_tc) e = cudaMemcpyAsync(&tc_status, bb->d_err, sizeof(int), cudaMemcpyDeviceToHost, h->stream);
 	if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
 	if (e != cudaSuccess) {
 		h->err = std::string("apply gates: ") + cudaGetErrorString(e);
+		return QCS_CUDA_ERROR;
+	}
+	if (tc_status != 0) {
+		h->err = tc_status == 1 ? "apply gates: a tensor-core block did not complete within its wait limit"
+		                        : "apply gates: a tile load did not complete within its wait limit";
 		return QCS_CUDA_ERROR;
 	}
 	return QCS_OK;
@@ -311,14 +379,23 @@ int run_planned(qcs_handle h, const std::vector<PlannedPass>& passes, int kmax, 
 
 }  // namespace
 
+// tile size of the fused path: tensor-core passes use tiles of kTcTileQubits
+int fused_tile_qubits(qcs_handle h) {
+	if (h->prec == QCS_FP64) return tile_qubits<double>();
+	return h->tensor_cores ? kTcTileQubits : tile_qubits<float>();
+}
+
 // dense blocks applied in shared-memory passes (the fused path and qcs_apply_matrix)
 int apply_blocks(qcs_handle h, std::vector<FusedBlock> blocks) {
 	const int n = static_cast<int>(h->n);
-	const int kfull = h->prec == QCS_FP64 ? tile_qubits<double>() : tile_qubits<float>();
-	const int kmax = std::min(kfull, n);
+	bool big = false;  // blocks of 4 or 5 qubits go to the tensor cores (FP32), whose passes use smaller tiles
+	for (const FusedBlock& b : blocks) big = big || b.qubits.size() >= 4;
+	const bool tc = h->prec == QCS_FP32 && h->tensor_cores && big;
+	const int kmax = std::min(tc ? kTcTileQubits : (h->prec == QCS_FP64 ? tile_qubits<double>() : tile_qubits<float>()), n);
 	const int L0 = std::min(n, std::max(5, kmax - 8));
 	std::vector<PlannedPass> passes(1);
 	passes.back().tmask = (1ULL << L0) - 1;
+	uint32_t tc_bytes = 0;  // resident tensor-core matrices of the open pass
 	for (FusedBlock& b : blocks) {
 		if (b.qubits.empty()) {  // a global factor only
 			h->scale *= b.M[0];
@@ -330,12 +407,15 @@ int apply_blocks(qcs_handle h, std::vector<FusedBlock> blocks) {
 		c.block_m = std::move(b.M);
 		c.block_gates = b.ngates;
 		const uint64_t need = c.local_mask();
-		if (popcount64(passes.back().tmask | need) > kmax) {
+		const uint32_t tcb = tc && c.block_q.size() >= 4 ? 32u << (2 * c.block_q.size()) : 0u;
+		if (popcount64(passes.back().tmask | need) > kmax || tc_bytes + tcb > kTcMatBudget) {
 			passes.emplace_back();
 			passes.back().tmask = ((1ULL << L0) - 1) | need;
+			tc_bytes = 0;
 		} else {
 			passes.back().tmask |= need;
 		}
+		tc_bytes += tcb;
 		passes.back().gates.push_back(std::move(c));
 	}
 	h->last_blocks = blocks.size();
@@ -350,8 +430,7 @@ int fused_apply(qcs_handle h, const qcs_gate* gates, size_t count) {
 	for (size_t i = 0; i < count; ++i) cg.push_back(compile_gate(gates[i], false));
 	std::vector<FusedBlock> blocks;
 	if (h->fusion == 2 && h->cost_ctx) {
-		const int kfull = h->prec == QCS_FP64 ? tile_qubits<double>() : tile_qubits<float>();
-		const int kmax = std::min(kfull, n);
+		const int kmax = std::min(fused_tile_qubits(h), n);
 		const int L0 = std::min(n, std::max(5, kmax - 8));
 		const int st = choose_partition(h, cg, kmax, L0, blocks, &h->last_predicted_ms);
 		if (st != QCS_OK) return st;
@@ -522,6 +601,7 @@ void batch_release(qcs_handle h) {
 	if (!bb) return;
 	if (bb->d_ops) cudaFree(bb->d_ops);
 	if (bb->d_mats) cudaFree(bb->d_mats);
+	if (bb->d_err) cudaFree(bb->d_err);
 	delete bb;
 	h->batch = nullptr;
 }

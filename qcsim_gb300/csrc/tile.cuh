@@ -12,7 +12,15 @@ namespace qcs {
 // PhaseRow: a QFT phase row (CompiledGate::PhaseRow): lbit1 = row_lo, lbit2 = row_bits, pad[0] = the
 // shift taking y to the table's 2^M-th roots, pad[1] = S, pad[2] = inverse, pad[3] = M; the factor
 // exp(2 pi i z / 2^M), z = y << shift, is table[mat + (z >> S)] * table[mat + 2^(M-S) + (z & (2^S - 1))]
-enum class TKind : uint8_t { Ctrl1q = 0, Swap = 1, Dense2 = 2, Dense3 = 3, GlobalDiag = 4, DenseN = 5, PhaseRow = 6 };
+// DenseTC: a fused 4- or 5-qubit block (FP32 registers) on the tensor cores; ins = its local positions,
+// mat = offset (complex entries, even) of its real-expanded 2D x 2D matrix as two TF32 splits in the
+// K-major operand layout (hi then lo, 16 D^2 bytes each), lbit1 = its byte offset in the kernel's
+// resident matrix area
+enum class TKind : uint8_t { Ctrl1q = 0, Swap = 1, Dense2 = 2, Dense3 = 3, GlobalDiag = 4, DenseN = 5, PhaseRow = 6, DenseTC = 7 };
+
+// tensor-core passes: tiles of exactly kTcTileQubits qubits; resident block matrices per pass
+constexpr int kTcTileQubits = 12;
+constexpr uint32_t kTcMatBudget = 65536;  // two 5-qubit blocks, or eight 4-qubit blocks
 
 // one gate inside a pass, in tile-local bit positions
 struct TileOp {
@@ -38,12 +46,13 @@ struct TilePass {
 	uint8_t high[32];      // global positions of local bits L..k-1
 	uint8_t fixed[40];     // global positions of the non-tile qubits, ascending
 	uint32_t op_begin, op_count;
-	int dense;             // the pass holds dense-block operations
+	int dense;             // 0: light operations only; 1: dense blocks on the CUDA cores; 2: tensor-core blocks
 };
 
+// d_err: set non-zero by a tensor-core pass whose bounded waits ran out (1: MMA completion, 2: tile load)
 template <typename T>
 cudaError_t launch_tile_pass(cplx_t<T>* s, const TilePass& p, const TileOp* d_ops, const cplx_t<T>* d_mats, int sms,
-                             cudaStream_t st);
+                             cudaStream_t st, int* d_err);
 
 // largest tile (qubits) for the precision, given the shared memory per block
 template <typename T> int tile_qubits();

@@ -1,13 +1,18 @@
 // Shared-memory pass kernel: each CTA loads a tile of 2^k amplitudes (contiguous runs of 2^L), applies
 // every gate of the pass with the same per-amplitude arithmetic as the per-gate kernels (gate_math.cuh),
 // and writes the tile back.  A persistent grid walks the 2^(n-k) tiles.
+#include <algorithm>
+
 #include "gate_math.cuh"
+#include "tcgen05.cuh"
 #include "tile.cuh"
 
 namespace qcs {
 namespace {
 
 constexpr int kTileThreads = 512;
+// tile loads in flight per thread (FP64 passes are FP64-pipe bound and keep their registers for occupancy)
+template <typename T> constexpr int load_batch() { return sizeof(T) == 4 ? 8 : 1; }
 constexpr int kMaxHigh = 8;  // at most 8 tile qubits above the contiguous low block
 
 // the loop-invariant fields of a TileOp, held in registers
@@ -132,8 +137,7 @@ __device__ __forceinline__ void tile_denseN(cplx_t<T>* sm, uint32_t items, const
 				if ((c >> j) & 1) x |= bits[j];
 			v[c] = sm[x];
 		}
-#pragma unroll 1
-		for (int r = 0; r < D; ++r) {
+		auto row_out = [&](int r) {
 			T re = 0, im = 0;
 			const cplx_t<T>* row = mats + op.mat + r * D;
 #pragma unroll
@@ -149,6 +153,18 @@ __device__ __forceinline__ void tile_denseN(cplx_t<T>* sm, uint32_t items, const
 			for (int j = 0; j < K; ++j)
 				if ((r >> j) & 1) x |= bits[j];
 			sm[x] = mk<T>(re, im);
+		};
+		// small FP32 blocks: several rows in flight at once (their matrix loads overlap); larger
+		// blocks one row at a time to bound the registers
+		if constexpr (K <= 2 && sizeof(T) == 4) {
+#pragma unroll
+			for (int r = 0; r < D; ++r) row_out(r);
+		} else if constexpr (K == 3 && sizeof(T) == 4) {
+#pragma unroll 2
+			for (int r = 0; r < D; ++r) row_out(r);
+		} else {
+#pragma unroll 1
+			for (int r = 0; r < D; ++r) row_out(r);
 		}
 	}
 }
@@ -255,10 +271,10 @@ __device__ __forceinline__ void tile_apply(cplx_t<T>* sm, int k, const TileOp& t
 	}
 }
 
-template <typename T, bool DENSE>
-__global__ void __launch_bounds__(kTileThreads) k_tile(cplx_t<T>* __restrict__ s, TilePass p, const TileOp* __restrict__ ops,
-                                                      const cplx_t<T>* __restrict__ mats, uint64_t ntiles) {
-	extern __shared__ __align__(16) unsigned char smraw[];
+template <typename T, bool DENSE, int THREADS>
+__global__ void __launch_bounds__(THREADS) k_tile(cplx_t<T>* __restrict__ s, TilePass p, const TileOp* __restrict__ ops,
+                                                 const cplx_t<T>* __restrict__ mats, uint64_t ntiles) {
+	extern __shared__ __align__(1024) unsigned char smraw[];
 	__shared__ uint64_t highoff[1 << kMaxHigh];
 	cplx_t<T>* sm = reinterpret_cast<cplx_t<T>*>(smraw);
 	const uint32_t K = 1u << p.k;
@@ -275,7 +291,20 @@ __global__ void __launch_bounds__(kTileThreads) k_tile(cplx_t<T>* __restrict__ s
 		uint64_t base = 0;
 		for (int j = 0; j < p.nfixed; ++j)
 			if ((tile >> j) & 1ULL) base |= 1ULL << p.fixed[j];
-		for (uint32_t j = threadIdx.x; j < K; j += blockDim.x) sm[j] = s[base | highoff[j >> p.L] | (j & lowmask)];
+		// loads in batches of load_batch per thread, all issued before the first shared-memory store
+		for (uint32_t j0 = threadIdx.x; j0 < K; j0 += blockDim.x * load_batch<T>()) {
+			cplx_t<T> r[load_batch<T>()];
+#pragma unroll
+			for (int b = 0; b < load_batch<T>(); ++b) {
+				const uint32_t j = j0 + b * blockDim.x;
+				if (j < K) r[b] = s[base | highoff[j >> p.L] | (j & lowmask)];
+			}
+#pragma unroll
+			for (int b = 0; b < load_batch<T>(); ++b) {
+				const uint32_t j = j0 + b * blockDim.x;
+				if (j < K) sm[j] = r[b];
+			}
+		}
 		__syncthreads();
 		for (uint32_t oi = 0; oi < p.op_count; ++oi) {
 			const TileOp op = ops[p.op_begin + oi];
@@ -283,9 +312,242 @@ __global__ void __launch_bounds__(kTileThreads) k_tile(cplx_t<T>* __restrict__ s
 			tile_apply<T, DENSE>(sm, p.k, op, mats, base, highoff, p.L);
 			__syncthreads();
 		}
-		for (uint32_t j = threadIdx.x; j < K; j += blockDim.x) s[base | highoff[j >> p.L] | (j & lowmask)] = sm[j];
+		for (uint32_t j0 = threadIdx.x; j0 < K; j0 += blockDim.x * load_batch<T>()) {
+			cplx_t<T> r[load_batch<T>()];
+#pragma unroll
+			for (int b = 0; b < load_batch<T>(); ++b) {
+				const uint32_t j = j0 + b * blockDim.x;
+				if (j < K) r[b] = sm[j];
+			}
+#pragma unroll
+			for (int b = 0; b < load_batch<T>(); ++b) {
+				const uint32_t j = j0 + b * blockDim.x;
+				if (j < K) s[base | highoff[j >> p.L] | (j & lowmask)] = r[b];
+			}
+		}
 		__syncthreads();
 	}
+}
+
+// ---- tensor-core passes (FP32 registers, fused 4- and 5-qubit blocks) ----
+//
+// A block of K qubits (D = 2^K) acts on the tile's C = 2^12 / D "columns" (assignments of the other
+// tile qubits).  As a real product: out (C x 2D) = in (C x 2D) * B (2D x 2D), in[c][2j + p] = part p of
+// amplitude j of column c, B[2j][2i] = Re M[i][j], B[2j + 1][2i] = -Im M[i][j], B[2j][2i + 1] = Im M[i][j],
+// B[2j + 1][2i + 1] = Re M[i][j].  Columns are the MMA's M dimension (tiles of 128 rows), 2D its N and
+// K.  3xTF32: each operand is split into TF32 hi + lo parts and out = in_hi B_hi + in_hi B_lo + in_lo B_hi,
+// accumulated in FP32 in tensor memory.
+//
+// Shared memory: the 32 KiB tile, the A operand (hi and lo splits) and the pass's block matrices (hi
+// and lo, kTcMatBudget bytes), loaded once per CTA.
+constexpr uint32_t kTcTileBytes = (1u << kTcTileQubits) * sizeof(float2);
+constexpr uint32_t kTcLboA = 144;     // A operand: a row's core matrices fall in different bank groups
+constexpr uint32_t kTcABytes = 36864;  // one split of A: 16 row groups x 16 core matrices x 144 bytes
+constexpr uint32_t kTcSmem = kTcTileBytes + 2 * kTcABytes + kTcMatBudget;
+constexpr uint32_t kTcTmemCols = 64;
+constexpr uint32_t kTcWaitTries = 1u << 22;
+
+__device__ __forceinline__ float tf32_rna(float x) {
+	uint32_t r;
+	asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
+	return __uint_as_float(r);
+}
+
+// the K block positions of a DenseTC op, ascending
+template <int K> struct BlockBits {
+	uint32_t pos[K];
+	__device__ __forceinline__ explicit BlockBits(uint64_t ins) {
+#pragma unroll
+		for (int t = 0; t < K; ++t) pos[t] = static_cast<uint32_t>((ins >> (8 * t)) & 0xffu);
+	}
+	// tile index -> column (the index without the block bits)
+	__device__ __forceinline__ uint32_t column(uint32_t x) const {
+#pragma unroll
+		for (int t = K - 1; t >= 0; --t) x = ((x >> (pos[t] + 1)) << pos[t]) | (x & ((1u << pos[t]) - 1));
+		return x;
+	}
+	// tile index -> block index j
+	__device__ __forceinline__ uint32_t index(uint32_t x) const {
+		uint32_t j = 0;
+#pragma unroll
+		for (int t = 0; t < K; ++t) j |= ((x >> pos[t]) & 1u) << t;
+		return j;
+	}
+	// (column, block index) -> tile index
+	__device__ __forceinline__ uint32_t place(uint32_t c, uint32_t j) const {
+#pragma unroll
+		for (int t = 0; t < K; ++t) c = ((c >> pos[t]) << (pos[t] + 1)) | (c & ((1u << pos[t]) - 1)) | (((j >> t) & 1u) << pos[t]);
+		return c;
+	}
+	__device__ __forceinline__ uint32_t low_count() const {
+		uint32_t n = 0;
+#pragma unroll
+		for (int t = 0; t < K; ++t) n += pos[t] < 5 ? 1u : 0u;
+		return n;
+	}
+};
+
+// applies one DenseTC op of K qubits to the tile; false when the MMA completion wait ran out
+template <int K>
+__device__ bool tile_block_tc(float2* sm, uint64_t ins, unsigned char* sA, const unsigned char* sBop, uint32_t tmem, uint64_t* mbar,
+                              uint32_t& phase) {
+	constexpr uint32_t D = 1u << K, kdim = 2 * D;
+	constexpr uint32_t sbo_a = (kdim / 4) * kTcLboA, sbo_b = (kdim / 4) * 128;
+	constexpr uint32_t cols = (1u << kTcTileQubits) >> K;  // 128 (K = 5) or 256 (K = 4)
+	constexpr uint32_t mt_bytes = 16 * sbo_a;                // one 128-row M tile of one split
+	const BlockBits<K> bb(ins);
+	// gather in tile order (conflict-free reads) into the A operand, split into TF32 hi and lo
+#pragma unroll 4
+	for (uint32_t x = threadIdx.x; x < (1u << kTcTileQubits); x += kTileThreads) {
+		const float2 v = sm[x];
+		const uint32_t c = bb.column(x), j = bb.index(x);
+		const float hx = tf32_rna(v.x), hy = tf32_rna(v.y);
+		const uint32_t off = (c >> 7) * mt_bytes + tc::kmajor_offset(c & 127u, 2 * j, kdim, kTcLboA);
+		*reinterpret_cast<float2*>(sA + off) = make_float2(hx, hy);
+		*reinterpret_cast<float2*>(sA + kTcABytes + off) = make_float2(tf32_rna(v.x - hx), tf32_rna(v.y - hy));
+	}
+	tc::fence_proxy_async();
+	tc::fence_before_sync();
+	__syncthreads();
+	tc::fence_after_sync();
+	if (threadIdx.x == 0) {
+		constexpr uint32_t idesc = tc::idesc_tf32(128, kdim);
+		const uint32_t a_hi = tc::smem_addr(sA), b_hi = tc::smem_addr(sBop);
+		// descriptors of k-step 0; each k-step advances the start address (16-byte units, low bits)
+		const uint64_t ah0 = tc::smem_desc(a_hi, kTcLboA, sbo_a), al0 = tc::smem_desc(a_hi + kTcABytes, kTcLboA, sbo_a);
+		const uint64_t bh0 = tc::smem_desc(b_hi, 128, sbo_b), bl0 = tc::smem_desc(b_hi + 16 * D * D, 128, sbo_b);
+#pragma unroll
+		for (uint32_t mt = 0; mt < cols / 128; ++mt) {
+#pragma unroll
+			for (uint32_t ks = 0; ks < kdim / 8; ++ks) {
+				const uint64_t da = (mt * mt_bytes + ks * 2 * kTcLboA) >> 4, db = (ks * 2 * 128) >> 4;
+				tc::mma_tf32(tmem + mt * kdim, ah0 + da, bh0 + db, idesc, ks > 0 ? 1u : 0u);
+				tc::mma_tf32(tmem + mt * kdim, ah0 + da, bl0 + db, idesc, 1u);
+				tc::mma_tf32(tmem + mt * kdim, al0 + da, bh0 + db, idesc, 1u);
+			}
+		}
+		tc::mma_commit(mbar);
+	}
+	const bool ok = tc::mbar_wait(mbar, phase, kTcWaitTries);
+	phase ^= 1u;
+	tc::fence_after_sync();
+	// warp w reads tensor-memory lanes 32 (w % 4) + 0..31 (M-tile rows = columns) and the 16
+	// accumulator columns 16 (w / 4) + 0..15 (8 complex outputs)
+	const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
+	const uint32_t quad = warp & 3u, cc = warp >> 2;
+	float v[16];
+	tc::tmem_ld16(tmem + ((32u * quad) << 16) + 16u * cc, v);
+	const uint32_t mt = (16u * cc) / kdim, i0 = ((16u * cc) % kdim) / 2;
+	const uint32_t c = mt * 128u + 32u * quad + lane;
+	// blocks on three or more of the five lowest tile bits: outputs go through a padded staging area
+	// (the A operand is free now) and back to the tile in tile order; otherwise straight to the tile
+	const bool staged = bb.low_count() >= 3;
+	if (!staged) {
+#pragma unroll
+		for (uint32_t t = 0; t < 8; ++t) sm[bb.place(c, i0 + t)] = make_float2(v[2 * t], v[2 * t + 1]);
+	} else {
+		float2* stage = reinterpret_cast<float2*>(sA);
+#pragma unroll
+		for (uint32_t t = 0; t < 8; ++t) stage[(i0 + t) * (cols + 1) + c] = make_float2(v[2 * t], v[2 * t + 1]);
+	}
+	tc::fence_before_sync();
+	if (staged) {
+		__syncthreads();
+		const float2* stage = reinterpret_cast<const float2*>(sA);
+#pragma unroll 4
+		for (uint32_t x = threadIdx.x; x < (1u << kTcTileQubits); x += kTileThreads) sm[x] = stage[bb.index(x) * (cols + 1) + bb.column(x)];
+	}
+	return ok;
+}
+
+__global__ void __launch_bounds__(kTileThreads, 1) k_tile_tc(float2* __restrict__ s, TilePass p, const TileOp* __restrict__ ops,
+                                                              const float2* __restrict__ mats, uint64_t ntiles, int* err) {
+	extern __shared__ __align__(1024) unsigned char smraw[];
+	__shared__ uint64_t highoff[1 << kMaxHigh];
+	__shared__ __align__(8) uint64_t mbar_mma;
+	__shared__ uint32_t tmem_slot;
+	__shared__ int stop;
+	float2* sm = reinterpret_cast<float2*>(smraw);
+	unsigned char* sA = smraw + kTcTileBytes;
+	unsigned char* sB = sA + 2 * kTcABytes;
+	const uint32_t warp = threadIdx.x >> 5;
+	const uint32_t lowmask = (1u << p.L) - 1;
+	const int nh = p.k - p.L;
+	for (uint32_t h = threadIdx.x; h < (1u << nh); h += blockDim.x) {
+		uint64_t off = 0;
+		for (int b = 0; b < nh; ++b)
+			if ((h >> b) & 1u) off |= 1ULL << p.high[b];
+		highoff[h] = off;
+	}
+	if (warp == 0) tc::tmem_alloc<kTcTmemCols>(&tmem_slot);
+	if (threadIdx.x == 0) {
+		tc::mbar_init(&mbar_mma, 1);
+		stop = 0;
+	}
+	// the pass's block matrices stay resident for every tile
+	for (uint32_t oi = 0; oi < p.op_count; ++oi) {
+		const TileOp& op = ops[p.op_begin + oi];
+		if (static_cast<TKind>(op.kind) != TKind::DenseTC) continue;
+		const uint32_t bytes = 32u << (2 * op.nins);
+		const uint4* src = reinterpret_cast<const uint4*>(mats + op.mat);
+		uint4* dst = reinterpret_cast<uint4*>(sB + op.lbit1);
+		for (uint32_t i = threadIdx.x; i < bytes / 16; i += blockDim.x) dst[i] = src[i];
+	}
+	tc::fence_proxy_async();
+	tc::fence_before_sync();
+	__syncthreads();
+	tc::fence_after_sync();
+	const uint32_t tmem = tmem_slot;
+	constexpr uint32_t kAmps = 1u << kTcTileQubits;
+	constexpr int kBatch = kAmps / kTileThreads;  // 8 loads in flight per thread
+	uint32_t mma_phase = 0;
+	for (uint64_t tile = blockIdx.x; tile < ntiles && !stop; tile += gridDim.x) {
+		uint64_t base = 0;
+		for (int j = 0; j < p.nfixed; ++j)
+			if ((tile >> j) & 1ULL) base |= 1ULL << p.fixed[j];
+		{
+			float2 r[kBatch];
+#pragma unroll
+			for (int b = 0; b < kBatch; ++b) {
+				const uint32_t j = threadIdx.x + b * kTileThreads;
+				r[b] = s[base | highoff[j >> p.L] | (j & lowmask)];
+			}
+#pragma unroll
+			for (int b = 0; b < kBatch; ++b) sm[threadIdx.x + b * kTileThreads] = r[b];
+		}
+		__syncthreads();
+		for (uint32_t oi = 0; oi < p.op_count; ++oi) {
+			const TileOp op = ops[p.op_begin + oi];
+			if ((base & op.gmask) != op.gmask) continue;
+			if (static_cast<TKind>(op.kind) == TKind::DenseTC) {
+				const bool ok = op.nins == 5 ? tile_block_tc<5>(sm, op.ins, sA, sB + op.lbit1, tmem, &mbar_mma, mma_phase)
+				                             : tile_block_tc<4>(sm, op.ins, sA, sB + op.lbit1, tmem, &mbar_mma, mma_phase);
+				if (!ok) {
+					atomicExch(err, 1);
+					stop = 1;
+				}
+			} else {
+				tile_apply<float, true>(sm, p.k, op, mats, base, highoff, p.L);
+			}
+			__syncthreads();
+			if (stop) break;
+		}
+		if (stop) break;
+		{
+			float2 r[kBatch];
+#pragma unroll
+			for (int b = 0; b < kBatch; ++b) r[b] = sm[threadIdx.x + b * kTileThreads];
+#pragma unroll
+			for (int b = 0; b < kBatch; ++b) {
+				const uint32_t j = threadIdx.x + b * kTileThreads;
+				s[base | highoff[j >> p.L] | (j & lowmask)] = r[b];
+			}
+		}
+		__syncthreads();
+	}
+	tc::fence_before_sync();
+	__syncthreads();
+	if (warp == 0) tc::tmem_dealloc<kTcTmemCols>(tmem);
 }
 
 }  // namespace
@@ -294,30 +556,52 @@ template <> int tile_qubits<double>() { return 12; }
 template <> int tile_qubits<float>() { return 13; }
 
 template <typename T>
-cudaError_t launch_tile_pass(cplx_t<T>* s, const TilePass& p, const TileOp* d_ops, const cplx_t<T>* d_mats, int sms, cudaStream_t st) {
-	static bool configured = false;
+cudaError_t launch_tile_pass(cplx_t<T>* s, const TilePass& p, const TileOp* d_ops, const cplx_t<T>* d_mats, int sms, cudaStream_t st,
+                             int* d_err) {
+	if constexpr (sizeof(T) == 4) {
+		if (p.dense == 2) {
+			static bool tc_configured = false;
+			if (!tc_configured) {
+				cudaError_t e = cudaFuncSetAttribute(k_tile_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(kTcSmem));
+				if (e != cudaSuccess) return e;
+				tc_configured = true;
+			}
+			if (p.k != kTcTileQubits || p.L < 5 || p.k - p.L > kMaxHigh || !d_err) return cudaErrorInvalidValue;
+			const uint64_t ntiles = 1ULL << p.nfixed;
+			const uint64_t grid = std::min<uint64_t>(static_cast<uint64_t>(sms), ntiles);
+			k_tile_tc<<<static_cast<unsigned>(grid), kTileThreads, kTcSmem, st>>>(s, p, d_ops, d_mats, ntiles, d_err);
+			note_launches(1);
+			return cudaGetLastError();
+		}
+	}
+	// dense FP32 passes need many registers: 256 threads per CTA so that two CTAs share an SM (one
+	// loading or storing its tile while the other computes)
+	constexpr int kDenseThreads = sizeof(T) == 4 ? 256 : kTileThreads;
+	auto* light = k_tile<T, false, kTileThreads>;
+	auto* dense = k_tile<T, true, kDenseThreads>;
+	static int per_sm[2] = {0, 0};
 	const size_t smem = (size_t(1) << p.k) * sizeof(cplx_t<T>);
-	if (!configured) {
+	if (!per_sm[0]) {
 		const int maxs = static_cast<int>((size_t(1) << tile_qubits<T>()) * sizeof(cplx_t<T>));
-		cudaError_t e = cudaFuncSetAttribute(k_tile<T, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, maxs);
-		if (e == cudaSuccess) e = cudaFuncSetAttribute(k_tile<T, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, maxs);
+		cudaError_t e = cudaFuncSetAttribute(light, cudaFuncAttributeMaxDynamicSharedMemorySize, maxs);
+		if (e == cudaSuccess) e = cudaFuncSetAttribute(dense, cudaFuncAttributeMaxDynamicSharedMemorySize, maxs);
+		// resident CTAs per SM at the largest tile (registers and shared memory both counted)
+		if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm[0], light, kTileThreads, static_cast<size_t>(maxs));
+		if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm[1], dense, kDenseThreads, static_cast<size_t>(maxs));
 		if (e != cudaSuccess) return e;
-		configured = true;
+		per_sm[0] = std::max(per_sm[0], 1);
+		per_sm[1] = std::max(per_sm[1], 1);
 	}
 	if (p.k - p.L > kMaxHigh || p.k > tile_qubits<T>()) return cudaErrorInvalidValue;
 	const uint64_t ntiles = 1ULL << p.nfixed;
-	int per_sm = static_cast<int>((200 * 1024) / (smem + 4096));
-	if (per_sm < 1) per_sm = 1;
-	if (per_sm > 4) per_sm = 4;
-	uint64_t grid = static_cast<uint64_t>(sms) * per_sm;
-	if (grid > ntiles) grid = ntiles;
-	if (p.dense) k_tile<T, true><<<static_cast<unsigned>(grid), kTileThreads, smem, st>>>(s, p, d_ops, d_mats, ntiles);
-	else k_tile<T, false><<<static_cast<unsigned>(grid), kTileThreads, smem, st>>>(s, p, d_ops, d_mats, ntiles);
+	const uint64_t grid = std::min<uint64_t>(static_cast<uint64_t>(sms) * per_sm[p.dense ? 1 : 0], ntiles);
+	if (p.dense) dense<<<static_cast<unsigned>(grid), kDenseThreads, smem, st>>>(s, p, d_ops, d_mats, ntiles);
+	else light<<<static_cast<unsigned>(grid), kTileThreads, smem, st>>>(s, p, d_ops, d_mats, ntiles);
 	note_launches(1);
 	return cudaGetLastError();
 }
 
-template cudaError_t launch_tile_pass<double>(double2*, const TilePass&, const TileOp*, const double2*, int, cudaStream_t);
-template cudaError_t launch_tile_pass<float>(float2*, const TilePass&, const TileOp*, const float2*, int, cudaStream_t);
+template cudaError_t launch_tile_pass<double>(double2*, const TilePass&, const TileOp*, const double2*, int, cudaStream_t, int*);
+template cudaError_t launch_tile_pass<float>(float2*, const TilePass&, const TileOp*, const float2*, int, cudaStream_t, int*);
 
 }  // namespace qcs

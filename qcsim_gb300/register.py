@@ -91,6 +91,11 @@ class QubitRegister:
         if max_qubits is not None:
             self._ck(self._lib.qcs_set_option(self._h, L.QCS_OPT_FUSION_MAX_QUBITS, int(max_qubits)))
 
+    def set_tensor_cores(self, enabled: bool) -> None:
+        """FP32 registers: fused 4- and 5-qubit blocks as 3xTF32 tensor-core products (default) or FP32
+        FMAs on the CUDA cores"""
+        self._ck(self._lib.qcs_set_option(self._h, L.QCS_OPT_TENSOR_CORES, int(bool(enabled))))
+
     def profile(self, enable: bool = True) -> None:
         """bracket every kernel launch of this register with CUDA events (see read_profile)"""
         self._ck(self._lib.qcs_profile_enable(self._h, int(bool(enable))))

@@ -400,6 +400,33 @@ def test_fused_fp32(Q, n, max_q):
     assert 1 - abs(np.vdot(want, got)) ** 2 < 1e-9
 
 
+@pytest.mark.parametrize("n,max_q,controlled", [(14, 5, 0.0), (16, 4, 0.1), (18, 5, 0.1), (20, 5, 0.0)])
+def test_fused_fp32_tensor_cores(Q, n, max_q, controlled):
+    """4- and 5-qubit fused blocks as 3xTF32 tensor-core products (tcgen05) against the FP64 oracle and
+    against the same blocks as FP32 FMAs on the CUDA cores: fidelity of the renormalised state within
+    1e-9, max amplitude error within 2e-6"""
+    from qcsim_gb300 import circuits
+    ops = circuits.layered_circuit(n, 8, seed=100 + n, p3=0.05, controlled_frac=controlled)
+    init = circuits.random_normal_state(n, n)
+    want = oracle_state(n, ops, init)
+    states = {}
+    for tc in (True, False):
+        reg = Q.QubitRegister(n, seed=1, precision="fp32")
+        reg.set_fusion(1, max_q)
+        reg.set_tensor_cores(tc)
+        reg.setRegisterStorageFastNoNormalize(init)
+        reg.profile(True)
+        reg.ApplyGates(ops)
+        prof = reg.read_profile()
+        assert ("tile_pass_tc" in prof) == tc, prof
+        got = reg.getRegisterStorage()
+        assert np.abs(got - want).max() < 2e-6, tc
+        got = got / np.linalg.norm(got)
+        assert 1 - abs(np.vdot(want, got)) ** 2 < 1e-9, tc
+        states[tc] = got
+    assert np.abs(states[True] - states[False]).max() < 2e-6
+
+
 def test_fused_fp64(Q):
     """fusion on an FP64 register (blocks of <= 4 qubits) stays within the FP64 tolerance"""
     from qcsim_gb300 import circuits, gates as G
