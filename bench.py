@@ -46,7 +46,8 @@ def parse():
     ap.add_argument("--model", default=None, help="learned config: cost-model file")
     ap.add_argument("--config", default="layered", choices=["layered", "precision", "qaoa", "learned"],
                     help="layered: the 30-qubit FP64 circuit (headline); precision: fused FP32 vs plain FP64")
-    ap.add_argument("--max-block", type=int, default=5, help="precision config: largest fused block")
+    ap.add_argument("--max-block", type=int, default=3, help="precision config: largest fused block")
+    ap.add_argument("--no-fused", action="store_true", help="skip the fused-FP32 comparison in the layered line")
     return ap.parse_args()
 
 
@@ -344,6 +345,13 @@ def run_gb300(args):
         extra["qft"] = {"qubits": n, "seconds": qft_ms / 1e3, "gates": len(qops), "gates_per_s": len(qops) / (qft_ms / 1e3),
                         "hbm_frac_per_gate": qb / (qft_ms / 1e3) / (peak * 1e9)}
 
+    # the metric's second half on the same circuit: its first four layers on a fresh FP64 register and on
+    # a fused FP32 register (greedy blocks of at most 3 qubits), device time and fidelity
+    if rank == 0 and not args.no_fused:
+        fops = [op for lay in layers[:4] for op in lay]
+        extra["fused_fp32"] = {"workload": f"layers 0-3 of the circuit above ({len(fops)} gates)",
+                               **fused_vs_fp64(n, fops, 3, args.seed)}
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         cpu = cpu_baseline(args, ops, rank)
@@ -401,25 +409,23 @@ def read_traffic(kernel_family: str, n: int):
     return None
 
 
-def run_precision(args):
-    """fused FP32 (dense blocks of <= max_block qubits) against plain FP64 on the same layered circuit:
-    device time of each and the fidelity / max amplitude error of the FP32 result"""
+def fused_vs_fp64(n: int, ops: list, max_block: int, seed: int = 1) -> dict:
+    """the same gate list on a plain FP64 register and on a fused FP32 register (greedy blocks of at most
+    max_block qubits; 4- and 5-qubit blocks on the tensor cores): device time of each (the call includes
+    the host-side planning) and the fidelity / max amplitude error of the FP32 result"""
     import ctypes as C
     import torch
     import qcsim_gb300 as Q
-    from qcsim_gb300 import _lib as L, circuits, gates as G
+    from qcsim_gb300 import _lib as L, gates as G
     lib = L.load()
-    n = args.qubits
-    ops = circuits.layered_circuit(n, args.depth, seed=args.seed)
     recs = G.records(ops)
     stream = torch.cuda.Stream()
-    out = {}
-    regs = {}
+    out, regs = {}, {}
     for prec in ("fp64", "fp32"):
-        reg = Q.QubitRegister(n, seed=args.seed, precision=prec)
+        reg = Q.QubitRegister(n, seed=seed, precision=prec)
         lib.qcs_set_stream(reg.handle, stream.cuda_stream)
         if prec == "fp32":
-            reg.set_fusion(1, args.max_block)
+            reg.set_fusion(1, max_block)
         reg.profile(True)
         torch.cuda.synchronize()
         a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -433,13 +439,24 @@ def run_precision(args):
         regs[prec] = reg
     f, d = C.c_double(), C.c_double()
     L.check(lib.qcs_compare(regs["fp64"].handle, regs["fp32"].handle, C.byref(f), C.byref(d)), regs["fp64"].handle)
+    for r in regs.values():
+        r.close()
+    return {"gates": len(ops), "max_block_qubits": max_block, "fp64_seconds": out["fp64"]["seconds"],
+            "fp32_fused_seconds": out["fp32"]["seconds"], "speedup": out["fp64"]["seconds"] / out["fp32"]["seconds"],
+            "one_minus_fidelity": 1.0 - f.value, "max_abs_amplitude_error": d.value,
+            "fp64_kernels": out["fp64"]["kernels"], "fp32_kernels": out["fp32"]["kernels"]}
+
+
+def run_precision(args):
+    """fused FP32 (dense blocks of <= max_block qubits) against plain FP64 on the same layered circuit"""
+    from qcsim_gb300 import circuits
+    n = args.qubits
+    ops = circuits.layered_circuit(n, args.depth, seed=args.seed)
+    res = fused_vs_fp64(n, ops, args.max_block, args.seed)
     line = {"metric": "fused FP32 vs plain FP64 time @1-F<=1e-6", "config": {
                 "workload": f"layered random circuit, {n} qubits, depth {args.depth}, seed {args.seed}",
-                "gates": len(ops), "max_block_qubits": args.max_block},
-            "fp64_seconds": out["fp64"]["seconds"], "fp32_fused_seconds": out["fp32"]["seconds"],
-            "speedup": out["fp64"]["seconds"] / out["fp32"]["seconds"], "one_minus_fidelity": 1.0 - f.value,
-            "max_abs_amplitude_error": d.value, "fp64_kernels": out["fp64"]["kernels"],
-            "fp32_kernels": out["fp32"]["kernels"], "data": "synthetic"}
+                "gates": res.pop("gates"), "max_block_qubits": res.pop("max_block_qubits")},
+            **res, "data": "synthetic"}
     print(json.dumps(line))
 
 

@@ -176,6 +176,12 @@ def sample_blocks(circuits: int, seed: int, nmin: int = 24, nmax: int = 32, dept
     return out
 
 
+def _pass_ms(prof: dict) -> float:
+    """average device time of the shared-memory passes in a profile (CUDA-core and tensor-core passes)"""
+    launches = sum(v[0] for k, v in prof.items() if k.startswith("tile_pass"))
+    return sum(v[1] for k, v in prof.items() if k.startswith("tile_pass")) / launches
+
+
 def time_blocks(samples, reps: int = 3, seed: int = 0, log=print) -> tuple[np.ndarray, np.ndarray, dict]:
     """device time of each sampled block applied alone in a pass, minus the time of a pass over the same
     register with a one-qubit identity (the memory cost every pass pays): returns features, log(ms)
@@ -197,7 +203,7 @@ def time_blocks(samples, reps: int = 3, seed: int = 0, log=print) -> tuple[np.nd
         for _ in range(reps):
             apply_matrix(reg, [0], eye)
         p = reg.read_profile()
-        base = p["tile_pass"][1] / p["tile_pass"][0]
+        base = _pass_ms(p)
         pass_ms[n] = base
         for (nn, qubits, ng) in by_n[n]:
             u = random_unitary(len(qubits), rng)
@@ -206,7 +212,7 @@ def time_blocks(samples, reps: int = 3, seed: int = 0, log=print) -> tuple[np.nd
             for _ in range(reps):
                 apply_matrix(reg, list(qubits), u)
             p = reg.read_profile()
-            ms = p["tile_pass"][1] / p["tile_pass"][0]
+            ms = _pass_ms(p)
             X.append(features(n, qubits, ng))
             T.append(math.log(max(ms - base, 0.02 * base)))
         reg.profile(False)
