@@ -90,3 +90,43 @@ def test_apply_matrix_any_order(cm):
         tol = 1e-12 if prec == "fp64" else 2e-6
         assert np.abs(reg.getRegisterStorage() - want).max() <= tol, (prec, k, qs)
     _ = (G, oracle_state)
+
+
+def test_trained_model_beats_the_fixed_fuser(cm):
+    """the committed, GPU-trained cost model against the method without it (the greedy fuser with its
+    default largest block of 5 qubits) on an unseen 26-qubit circuit with controlled rotations: the
+    learned partition must run faster, and both FP32 results stay within 1-F <= 1e-6 of the FP64 path"""
+    import ctypes as C
+    import torch
+    from qcsim_gb300 import QubitRegister, _lib as L, circuits, gates as G
+    lib = L.load()
+    n = 26
+    ops = circuits.layered_circuit(n, 12, seed=4242, controlled_frac=0.1)
+    recs = G.records(ops)
+    mlp, pass_ms = cm.load()
+    ref = QubitRegister(n, seed=1)
+    ref.apply_records(recs)
+
+    def run(setup):
+        reg = QubitRegister(n, seed=1, precision="fp32")
+        setup(reg)
+        reg.apply_records(recs)  # planning and first-touch warm-up
+        best = 1e9
+        for _ in range(3):
+            reg.setToBasisState(0)
+            torch.cuda.synchronize()
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record()
+            reg.apply_records(recs)
+            b.record()
+            b.synchronize()
+            best = min(best, a.elapsed_time(b))
+        f, d = C.c_double(), C.c_double()
+        L.check(lib.qcs_compare(ref.handle, reg.handle, C.byref(f), C.byref(d)), ref.handle)
+        reg.close()
+        return best, 1.0 - f.value
+
+    t_greedy, inf_greedy = run(lambda r: r.set_fusion(1, 5))
+    t_learned, inf_learned = run(lambda r: cm.attach(r, mlp, pass_ms))
+    assert inf_greedy <= 1e-6 and inf_learned <= 1e-6
+    assert t_learned < 0.8 * t_greedy, (t_learned, t_greedy)

@@ -162,3 +162,17 @@ def test_block_features_layout():
     assert f.shape == (costmodel.F,)
     assert f[0] == pytest.approx(3 / 5) and f[1] == pytest.approx(7 / 32) and f[2] == pytest.approx(30 / 32)
     assert f[5] == pytest.approx(1 / 5) and f[6] == pytest.approx(1 / 5) and f[10] == 1
+
+
+def test_committed_cost_model_is_sane():
+    """the GPU-trained cost model shipped with the package: its parameters load, the CPU restatement of
+    the network predicts finite block times, a 5-qubit block costs more than a 1-qubit block, and the
+    per-size pass times double with each qubit"""
+    from qcsim_gb300 import costmodel as cm
+    d = np.load(cm.MODEL_DIR / "fusion_cost_mlp.npz")
+    ref = cm.MlpRef(d["params"].astype(np.float64))
+    x = np.stack([cm.features(30, [3], 1), cm.features(30, [2, 7, 11, 20, 29], 6)]).astype(np.float64)
+    y = ref.forward(x).reshape(-1)
+    assert np.all(np.isfinite(y)) and y[1] > y[0]
+    pm = d["pass_ms"]
+    assert all(1.6 < pm[n + 1] / pm[n] < 2.4 for n in range(24, 32))
