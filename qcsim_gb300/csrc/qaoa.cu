@@ -11,10 +11,17 @@
 // <H> = sum_x |psi_x|^2 E(x), E(x) = -(sum h_q s_q + sum J_ij s_i s_j) (IsingModel.h:106-119, 203-206),
 // is reduced in FP64 in a fixed order.
 //
+// K(x) is never summed edge by edge per amplitude.  With the qubits split into the low group (the
+// first g0 = min(n, 12) qubits, one tile) and the high group, K = K_low(x_low) + K_high(x_high) +
+// sum_{i low} s_i c_i(x_high), c_i = sum of J_ij s_j over i's edges into the high group.  K_low is a
+// per-instance table; per tile (x_high fixed) K_high and the c_i are computed once, and the cross
+// term comes from two 64-entry tables over the low group's two 6-bit halves.
+//
 // Work split: instances sorted by size (largest first) are dealt round-robin to thread-block
 // clusters; the CTAs of a cluster share an instance's tiles and meet at a cluster barrier between
 // passes.  No CTA waits on another cluster, so the kernel needs no inter-CTA flags.
 #include <algorithm>
+#include <array>
 #include <cmath>
 #include <complex>
 #include <cstring>
@@ -46,6 +53,9 @@ struct QInst {
 	uint32_t kmax;         // sum |J|
 	uint32_t tab;          // complex-table offset: per layer [2*kmax+1] + [2^g0] + [2^(n-g0)]
 	uint32_t eh;           // double-table offset: [2^g0] + [2^(n-g0)] field energies
+	uint32_t kl;           // int16-table offset: [2^g0] K over the edges inside the low group
+	uint16_t nlow, nhigh;  // edges [0, nlow) inside the low group, [nlow, nlow + nhigh) inside the high
+	                       // group, the rest cross the groups with ei low and ej high
 	uint8_t ei[kMaxEdges], ej[kMaxEdges];
 	int8_t J[kMaxEdges];
 	uint32_t tab_stride;   // complex entries per layer
@@ -66,6 +76,7 @@ template <typename T> struct QParams {
 	uint32_t p;
 	const cplx_t<T>* tabs;
 	const double* etab;
+	const int16_t* kltab;
 	const QLayer* layers;         // [inst][layer]
 	double* parts;                // energy partials
 	double* energies;             // out
@@ -109,11 +120,83 @@ __device__ void rx_local(cplx_t<T>* sm, uint32_t k, uint32_t lo, uint32_t hi, co
 	}
 }
 
+// tile loads and stores with several loads in flight per thread
+template <typename T> constexpr int qaoa_batch() { return sizeof(T) == 4 ? 4 : 2; }
+
 template <typename T>
-__global__ void __launch_bounds__(kQThreads) k_qaoa(QParams<T> P) {
+__device__ __forceinline__ void tile_load(cplx_t<T>* sm, const cplx_t<T>* s, const TileGeo& G, uint64_t t, uint32_t K) {
+	constexpr int B = qaoa_batch<T>();
+	for (uint32_t j0 = threadIdx.x; j0 < K; j0 += kQThreads * B) {
+		cplx_t<T> r[B];
+#pragma unroll
+		for (int b = 0; b < B; ++b) {
+			const uint32_t j = j0 + b * kQThreads;
+			if (j < K) r[b] = s[G.addr(t, j)];
+		}
+#pragma unroll
+		for (int b = 0; b < B; ++b) {
+			const uint32_t j = j0 + b * kQThreads;
+			if (j < K) sm[j] = r[b];
+		}
+	}
+}
+
+template <typename T>
+__device__ __forceinline__ void tile_store(const cplx_t<T>* sm, cplx_t<T>* s, const TileGeo& G, uint64_t t, uint32_t K) {
+	constexpr int B = qaoa_batch<T>();
+	for (uint32_t j0 = threadIdx.x; j0 < K; j0 += kQThreads * B) {
+		cplx_t<T> r[B];
+#pragma unroll
+		for (int b = 0; b < B; ++b) {
+			const uint32_t j = j0 + b * kQThreads;
+			if (j < K) r[b] = sm[j];
+		}
+#pragma unroll
+		for (int b = 0; b < B; ++b) {
+			const uint32_t j = j0 + b * kQThreads;
+			if (j < K) s[G.addr(t, j)] = r[b];
+		}
+	}
+}
+
+// per tile of the low-group geometry (x_high = t): K_high and the cross-term tables kc[0..63] (low
+// bits 0-5) and kc[64..127] (low bits 6-11); ends with a barrier
+__device__ __forceinline__ void cross_tables(const QInst& I, uint64_t t, int* kc, int* khigh, int* cvec) {
+	const uint32_t g0 = I.g0;
+	if (threadIdx.x < g0) {
+		int c = 0;
+		for (uint32_t e = I.nlow + I.nhigh; e < I.nedges; ++e)
+			if (I.ei[e] == threadIdx.x) c += ((t >> (I.ej[e] - g0)) & 1ULL) ? -I.J[e] : I.J[e];
+		cvec[threadIdx.x] = c;
+	} else if (threadIdx.x == 32) {
+		int k = 0;
+		for (uint32_t e = I.nlow; e < I.nlow + I.nhigh; ++e) {
+			const uint64_t par = ((t >> (I.ei[e] - g0)) ^ (t >> (I.ej[e] - g0))) & 1ULL;
+			k += par ? -I.J[e] : I.J[e];
+		}
+		*khigh = k;
+	}
+	__syncthreads();
+	if (threadIdx.x < 128) {
+		const uint32_t half = threadIdx.x >> 6, u = threadIdx.x & 63u;
+		int k = 0;
+		for (uint32_t b = 0; b < 6; ++b) {
+			const uint32_t q = 6 * half + b;
+			if (q < g0) k += ((u >> b) & 1u) ? -cvec[q] : cvec[q];
+		}
+		kc[threadIdx.x] = k;
+	}
+	__syncthreads();
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kQThreads, 2) k_qaoa(QParams<T> P) {
 	extern __shared__ __align__(16) unsigned char smraw[];
 	cplx_t<T>* sm = reinterpret_cast<cplx_t<T>*>(smraw);
 	__shared__ double red[kQThreads];
+	__shared__ int kc[128];
+	__shared__ int cvec[kGroupBits];
+	__shared__ int khigh;
 	cg::cluster_group cluster = cg::this_cluster();
 	const uint32_t crank = cluster.block_rank();
 	const uint32_t csize = cluster.num_blocks();
@@ -125,88 +208,77 @@ __global__ void __launch_bounds__(kQThreads) k_qaoa(QParams<T> P) {
 		const uint32_t n = I.n;
 		const uint32_t g0 = I.g0;
 		const uint32_t nstages = (n > g0) ? ((n - g0 + 5) / 6) : 0;  // high-qubit mixer passes
-		double partial_total = 0;
+		const int16_t* KL = P.kltab + I.kl;
+		TileGeo G0;  // the low-group geometry: tile = x_low, tile index = x_high
+		G0.n = n; G0.L = g0; G0.hq0 = g0; G0.nh = 0;
 		for (uint32_t l = 0; l < P.p; ++l) {
 			const QLayer Lr = P.layers[static_cast<size_t>(P.order[w]) * P.p + l];
 			const cplx_t<T>* tabJ = P.tabs + I.tab + static_cast<size_t>(l) * I.tab_stride;
 			const cplx_t<T>* tab0 = tabJ + (2 * I.kmax + 1);
 			const cplx_t<T>* tab1 = tab0 + (1u << g0);
-			const bool last_layer = (l + 1 == P.p);
 			for (uint32_t stage = 0; stage <= nstages; ++stage) {
-				TileGeo G;
-				G.n = n;
-				if (stage == 0) {
-					G.L = g0; G.hq0 = g0; G.nh = 0;
-				} else {
+				TileGeo G = G0;
+				if (stage > 0) {
 					const uint32_t lo = g0 + 6 * (stage - 1);
 					G.L = 6; G.hq0 = lo; G.nh = min(6u, n - lo);
 				}
 				const uint64_t ntiles = G.ntiles();
 				const uint32_t K = G.size();
-				const bool final_pass = last_layer && stage == nstages;
 				for (uint64_t t = crank; t < ntiles; t += csize) {
-					for (uint32_t j = threadIdx.x; j < K; j += blockDim.x) sm[j] = s[G.addr(t, j)];
-					__syncthreads();
+					tile_load<T>(sm, s, G, t, K);
 					if (stage == 0) {
 						// the Ising operator on every amplitude of the tile, then RX on the low qubits
+						cross_tables(I, t, kc, &khigh, cvec);
+						const int kbase = khigh + static_cast<int>(I.kmax);
+						const cplx_t<T> fh = tab1[t];
 						for (uint32_t j = threadIdx.x; j < K; j += blockDim.x) {
-							const uint64_t x = G.addr(t, j);
-							int kk = 0;
-							for (uint32_t e = 0; e < I.nedges; ++e) {
-								const int par = static_cast<int>(((x >> I.ei[e]) ^ (x >> I.ej[e])) & 1ULL);
-								kk += par ? -I.J[e] : I.J[e];
-							}
-							cplx_t<T> f = cmul<T>(tabJ[kk + static_cast<int>(I.kmax)], tab0[x & ((1u << g0) - 1)]);
-							f = cmul<T>(f, tab1[x >> g0]);
+							const int kk = KL[j] + kbase + kc[j & 63u] + kc[64 + (j >> 6)];
+							const cplx_t<T> f = cmul<T>(cmul<T>(tabJ[kk], tab0[j]), fh);
 							sm[j] = cmul<T>(sm[j], f);
 						}
 						__syncthreads();
 						rx_local<T>(sm, G.L, 0, G.L, Lr);
 					} else {
+						__syncthreads();
 						rx_local<T>(sm, G.L + G.nh, G.L, G.L + G.nh, Lr);
 					}
-					if (final_pass) {
-						// <H> partial of this tile: sum |a|^2 E(x)
-						double acc = 0;
-						const double* eh0 = P.etab + I.eh;
-						const double* eh1 = eh0 + (1u << g0);
-						for (uint32_t j = threadIdx.x; j < K; j += blockDim.x) {
-							const uint64_t x = G.addr(t, j);
-							int kk = 0;
-							for (uint32_t e = 0; e < I.nedges; ++e) {
-								const int par = static_cast<int>(((x >> I.ei[e]) ^ (x >> I.ej[e])) & 1ULL);
-								kk += par ? -I.J[e] : I.J[e];
-							}
-							const double E = -(static_cast<double>(kk) + eh0[x & ((1u << g0) - 1)] + eh1[x >> g0]);
-							const double ax = sm[j].x, ay = sm[j].y;
-							acc += (ax * ax + ay * ay) * E;
-						}
-						red[threadIdx.x] = acc;
-						__syncthreads();
-						for (int wdt = blockDim.x / 2; wdt > 0; wdt >>= 1) {
-							if (threadIdx.x < wdt) red[threadIdx.x] += red[threadIdx.x + wdt];
-							__syncthreads();
-						}
-						if (threadIdx.x == 0) P.parts[I.part_offset + t] = red[0];
-						__syncthreads();
-					}
-					for (uint32_t j = threadIdx.x; j < K; j += blockDim.x) s[G.addr(t, j)] = sm[j];
+					tile_store<T>(sm, s, G, t, K);
 					__syncthreads();
 				}
 				cluster.sync();
-				(void)partial_total;
 			}
+		}
+		// <H> = sum |a|^2 E(x): one read-only pass in the low-group geometry, partials per tile
+		{
+			const double* eh0 = P.etab + I.eh;
+			const double* eh1 = eh0 + (1u << g0);
+			const uint64_t ntiles = G0.ntiles();
+			const uint32_t K = G0.size();
+			for (uint64_t t = crank; t < ntiles; t += csize) {
+				tile_load<T>(sm, s, G0, t, K);
+				cross_tables(I, t, kc, &khigh, cvec);
+				const double ebase = static_cast<double>(khigh) + eh1[t];
+				double acc = 0;
+				for (uint32_t j = threadIdx.x; j < K; j += blockDim.x) {
+					const int kk = KL[j] + kc[j & 63u] + kc[64 + (j >> 6)];
+					const double E = -(static_cast<double>(kk) + ebase + eh0[j]);
+					const double ax = sm[j].x, ay = sm[j].y;
+					acc += (ax * ax + ay * ay) * E;
+				}
+				red[threadIdx.x] = acc;
+				__syncthreads();
+				for (int wdt = blockDim.x / 2; wdt > 0; wdt >>= 1) {
+					if (threadIdx.x < wdt) red[threadIdx.x] += red[threadIdx.x + wdt];
+					__syncthreads();
+				}
+				if (threadIdx.x == 0) P.parts[I.part_offset + t] = red[0];
+				__syncthreads();
+			}
+			cluster.sync();
 		}
 		// fixed-order final reduction by the cluster's first CTA
 		if (crank == 0) {
-			TileGeo G;
-			G.n = n;
-			if (nstages == 0) { G.L = g0; G.hq0 = g0; G.nh = 0; }
-			else {
-				const uint32_t lo = g0 + 6 * (nstages - 1);
-				G.L = 6; G.hq0 = lo; G.nh = min(6u, n - lo);
-			}
-			const uint64_t ntiles = G.ntiles();
+			const uint64_t ntiles = G0.ntiles();
 			double acc = 0;
 			for (uint64_t t = threadIdx.x; t < ntiles; t += blockDim.x) acc += P.parts[I.part_offset + t];
 			red[threadIdx.x] = acc;
@@ -241,6 +313,8 @@ struct qcs_qaoa_batch {
 	uint32_t* d_order = nullptr;
 	void* d_tabs = nullptr;
 	double* d_etab = nullptr;
+	int16_t* d_kltab = nullptr;
+	size_t kl_entries = 0;
 	qcs::QLayer* d_layers = nullptr;
 	double* d_parts = nullptr;
 	double* d_energies = nullptr;
@@ -279,6 +353,7 @@ cudaError_t launch(qcs_qaoa_batch* b) {
 	P.p = b->p;
 	P.tabs = static_cast<const qcs::cplx_t<T>*>(b->d_tabs);
 	P.etab = b->d_etab;
+	P.kltab = b->d_kltab;
 	P.layers = b->d_layers;
 	P.parts = b->d_parts;
 	P.energies = b->d_energies;
@@ -354,6 +429,8 @@ int qcs_qaoa_batch_create(const qcs_qaoa_instance* instances, size_t count, uint
 		I.nedges = in.nedges;
 		I.g0 = std::min<uint32_t>(in.n, qcs::kGroupBits);
 		int ksum = 0;
+		// edges grouped: inside the low group, inside the high group, across (low end first)
+		std::vector<std::array<int, 3>> lowe, highe, crosse;
 		for (uint32_t e = 0; e < in.nedges; ++e) {
 			const double J = in.J[e];
 			if (J != std::floor(J) || std::abs(J) > 16 || in.edges[2 * e] >= in.n || in.edges[2 * e + 1] >= in.n ||
@@ -361,11 +438,25 @@ int qcs_qaoa_batch_create(const qcs_qaoa_instance* instances, size_t count, uint
 				delete b;
 				return QCS_UNSUPPORTED;  // the batch kernel takes small integer couplings
 			}
-			I.ei[e] = static_cast<uint8_t>(in.edges[2 * e]);
-			I.ej[e] = static_cast<uint8_t>(in.edges[2 * e + 1]);
-			I.J[e] = static_cast<int8_t>(J);
+			int a = static_cast<int>(in.edges[2 * e]), c = static_cast<int>(in.edges[2 * e + 1]);
+			const bool al = a < static_cast<int>(I.g0), cl = c < static_cast<int>(I.g0);
+			if (al && cl) lowe.push_back({a, c, static_cast<int>(J)});
+			else if (!al && !cl) highe.push_back({a, c, static_cast<int>(J)});
+			else crosse.push_back(al ? std::array<int, 3>{a, c, static_cast<int>(J)} : std::array<int, 3>{c, a, static_cast<int>(J)});
 			ksum += static_cast<int>(std::abs(J));
 		}
+		uint32_t e = 0;
+		for (const auto* group : {&lowe, &highe, &crosse})
+			for (const auto& x : *group) {
+				I.ei[e] = static_cast<uint8_t>(x[0]);
+				I.ej[e] = static_cast<uint8_t>(x[1]);
+				I.J[e] = static_cast<int8_t>(x[2]);
+				++e;
+			}
+		I.nlow = static_cast<uint16_t>(lowe.size());
+		I.nhigh = static_cast<uint16_t>(highe.size());
+		I.kl = static_cast<uint32_t>(b->kl_entries);
+		b->kl_entries += 1u << I.g0;
 		if (ksum > qcs::kMaxK) {
 			delete b;
 			return QCS_UNSUPPORTED;
@@ -380,15 +471,7 @@ int qcs_qaoa_batch_create(const qcs_qaoa_instance* instances, size_t count, uint
 		I.eh = static_cast<uint32_t>(b->etab_entries);
 		b->etab_entries += (1u << I.g0) + (1u << (in.n - I.g0));
 		I.part_offset = b->total_parts;
-		// tiles of the final pass
-		const uint32_t nst = (I.n > I.g0) ? ((I.n - I.g0 + 5) / 6) : 0;
-		uint32_t L = I.g0, nh = 0;
-		if (nst) {
-			const uint32_t lo = I.g0 + 6 * (nst - 1);
-			L = 6;
-			nh = std::min(6u, I.n - lo);
-		}
-		b->total_parts += 1ULL << (I.n - L - nh);
+		b->total_parts += 1ULL << (I.n - I.g0);  // one energy partial per low-group tile
 	}
 	b->order.resize(count);
 	std::iota(b->order.begin(), b->order.end(), 0u);
@@ -403,6 +486,20 @@ int qcs_qaoa_batch_create(const qcs_qaoa_instance* instances, size_t count, uint
 	if (e == cudaSuccess) e = cudaMalloc(&b->d_order, count * sizeof(uint32_t));
 	if (e == cudaSuccess) e = cudaMalloc(&b->d_tabs, b->tab_entries * ab);
 	if (e == cudaSuccess) e = cudaMalloc(&b->d_etab, b->etab_entries * sizeof(double));
+	if (e == cudaSuccess) e = cudaMalloc(&b->d_kltab, b->kl_entries * sizeof(int16_t));
+	// K over the low group's internal edges for every low-group pattern
+	if (e == cudaSuccess) {
+		std::vector<int16_t> kl(b->kl_entries);
+		for (size_t i = 0; i < count; ++i) {
+			const qcs::QInst& I = b->inst[i];
+			for (uint32_t x = 0; x < (1u << I.g0); ++x) {
+				int k = 0;
+				for (uint32_t q = 0; q < I.nlow; ++q) k += (((x >> I.ei[q]) ^ (x >> I.ej[q])) & 1u) ? -I.J[q] : I.J[q];
+				kl[I.kl + x] = static_cast<int16_t>(k);
+			}
+		}
+		e = cudaMemcpy(b->d_kltab, kl.data(), kl.size() * sizeof(int16_t), cudaMemcpyHostToDevice);
+	}
 	if (e == cudaSuccess) e = cudaMalloc(&b->d_layers, count * p * sizeof(qcs::QLayer));
 	if (e == cudaSuccess) e = cudaMalloc(&b->d_parts, std::max<uint64_t>(1, b->total_parts) * sizeof(double));
 	if (e == cudaSuccess) e = cudaMalloc(&b->d_energies, count * sizeof(double));
@@ -587,6 +684,7 @@ int qcs_qaoa_batch_destroy(qcs_qaoa_batch_handle b) {
 	cudaFree(b->d_order);
 	cudaFree(b->d_tabs);
 	cudaFree(b->d_etab);
+	cudaFree(b->d_kltab);
 	cudaFree(b->d_layers);
 	cudaFree(b->d_parts);
 	cudaFree(b->d_energies);
