@@ -470,17 +470,7 @@ def run_qaoa(args):
     out = {}
     for prec in ("fp64", "fp32"):
         batch = qaoa.QaoaBatch(insts, 4, prec)
-        best = None
-        for cl in (1, 2, 4, 8):  # the schedule shape, chosen by timing (autotune)
-            batch.set_cluster(cl)
-            batch.run()
-            torch.cuda.synchronize()
-            t0 = time.perf_counter()
-            batch.run()
-            dt = time.perf_counter() - t0
-            if best is None or dt < best[1]:
-                best = (cl, dt)
-        batch.set_cluster(best[0])
+        tuned = batch.autotune()  # the schedule shape (cluster size), chosen by timing
         batch.run()
         times = []
         for _ in range(max(3, args.steps // 5)):
@@ -488,7 +478,7 @@ def run_qaoa(args):
             e = batch.run()
             times.append(time.perf_counter() - t0)
         amps = batch.amplitudes
-        out[prec] = {"cluster": best[0], "seconds_per_launch": statistics.median(times),
+        out[prec] = {"cluster": batch.cluster, "autotune_seconds": tuned, "seconds_per_launch": statistics.median(times),
                      "instances_per_s": len(insts) / statistics.median(times),
                      "amplitude_layers_per_s": amps * 4 / statistics.median(times), "energies": e}
         batch.close()

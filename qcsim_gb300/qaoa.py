@@ -6,10 +6,15 @@ IsingModel.h:569-578)."""
 from __future__ import annotations
 
 import ctypes as C
+import json
+import time
+from pathlib import Path
 
 import numpy as np
 
 from . import _lib as L
+
+CLUSTER_SIZES = (1, 2, 4, 8)  # CTAs per thread-block cluster (portable sizes)
 
 
 class QaoaBatch:
@@ -30,6 +35,8 @@ class QaoaBatch:
             arr[i].J = J.ctypes.data_as(C.POINTER(C.c_double))
             arr[i].h = h.ctypes.data_as(C.POINTER(C.c_double))
         self._h = C.c_void_p()
+        self.precision = precision
+        self.cluster = 0
         prec = L.QCS_FP64 if precision == "fp64" else L.QCS_FP32
         L.check(self._lib.qcs_qaoa_batch_create(C.cast(arr, C.c_void_p), len(instances), p, prec, C.byref(self._h)))
         self.set_angles(np.array([inst["gammas"] for inst in instances]), np.array([inst["betas"] for inst in instances]))
@@ -45,6 +52,43 @@ class QaoaBatch:
 
     def set_cluster(self, ctas: int) -> None:
         self._ck(self._lib.qcs_qaoa_batch_set_cluster(self._h, ctas))
+        self.cluster = ctas
+
+    def shape_key(self, precision: str | None = None) -> str:
+        """what the schedule depends on: precision, layer count and the instance-size histogram"""
+        sizes: dict[int, int] = {}
+        for inst in self.instances:
+            sizes[inst["n"]] = sizes.get(inst["n"], 0) + 1
+        hist = ",".join(f"{n}:{c}" for n, c in sorted(sizes.items()))
+        return f"{precision or self.precision}|p{self.p}|{hist}"
+
+    def autotune(self, candidates=CLUSTER_SIZES, reps: int = 2, cache: Path | None = None) -> dict:
+        """choose the cluster size (CTAs that share one instance's tiles) by timing one launch of each
+        candidate after a warm-up launch, keep the fastest, and return {size: seconds}.  With `cache`
+        (a JSON file), a choice recorded for the same shape key is reused without timing."""
+        key = self.shape_key()
+        table = {}
+        if cache is not None and Path(cache).exists():
+            table = json.loads(Path(cache).read_text())
+            if key in table:
+                self.set_cluster(int(table[key]["cluster"]))
+                return {int(k): v for k, v in table[key]["seconds"].items()}
+        times = {}
+        for cl in candidates:
+            self.set_cluster(cl)
+            self.run()  # graph capture and warm-up
+            best = float("inf")
+            for _ in range(reps):
+                t0 = time.perf_counter()
+                self.run()
+                best = min(best, time.perf_counter() - t0)
+            times[cl] = best
+        choice = min(times, key=times.get)
+        self.set_cluster(choice)
+        if cache is not None:
+            table[key] = {"cluster": choice, "seconds": times}
+            Path(cache).write_text(json.dumps(table, indent=1))
+        return times
 
     def run(self) -> np.ndarray:
         out = np.empty(len(self.instances), dtype=np.float64)

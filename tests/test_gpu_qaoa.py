@@ -76,3 +76,26 @@ def test_batch_new_angles(qaoa):
         _, e = oracle_run(inst2)
         assert abs(e2[i] - e) <= 1e-10
     assert not np.allclose(e1, e2)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_autotune_schedule_invariant(qaoa, precision, tmp_path):
+    """the autotuner times every cluster size and keeps the fastest; every schedule gives the same
+    energies bit for bit (fixed-order reductions), and a cached choice is reused without timing"""
+    from qcsim_gb300 import circuits
+    insts = circuits.qaoa_instances(24, seed=11, nmin=10, nmax=18, p=2)
+    batch = qaoa.QaoaBatch(insts, 2, precision)
+    energies = {}
+    for cl in qaoa.CLUSTER_SIZES:
+        batch.set_cluster(cl)
+        energies[cl] = batch.run()
+    ref = energies[qaoa.CLUSTER_SIZES[0]]
+    for cl, e in energies.items():
+        assert np.array_equal(e, ref), cl
+    cache = tmp_path / "qaoa_schedule.json"
+    times = batch.autotune(cache=cache)
+    assert set(times) == set(qaoa.CLUSTER_SIZES)
+    assert batch.cluster == min(times, key=times.get)
+    assert np.array_equal(batch.run(), ref)
+    other = qaoa.QaoaBatch(insts, 2, precision)
+    assert other.autotune(cache=cache) == times and other.cluster == batch.cluster
