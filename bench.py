@@ -142,12 +142,8 @@ def barrier(dist):
 
 
 def max_over_ranks(dist, v: float) -> float:
-    if dist is None:
-        return v
-    import torch
-    t = torch.tensor([v], dtype=torch.float64, device="cuda")
-    dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    return float(t.item())
+    from qcsim_gb300 import replicas
+    return replicas.max_over_ranks(dist, v, device="cuda")
 
 
 def layers_of(ops, n):
@@ -464,24 +460,33 @@ def run_qaoa(args):
     """512 random 3-regular Ising instances (n even in 12..24), p = 4: <H> for every instance per graph
     launch, FP64 and FP32; instances/s and amplitude-layer updates/s"""
     import torch
-    from qcsim_gb300 import circuits, qaoa
+    from qcsim_gb300 import circuits, qaoa, replicas
     from oracle import bind as B
+    rank, world, local, dist = dist_init(args)
     insts = circuits.qaoa_instances(512, seed=args.seed, nmin=12, nmax=24, p=4)
+    # instances dealt to ranks by cost; each rank runs its share in one launch, energies gathered at the end
+    mine = replicas.shard_by_cost(replicas.qaoa_costs(insts), world)[rank]
     out = {}
     for prec in ("fp64", "fp32"):
-        batch = qaoa.QaoaBatch(insts, 4, prec)
+        batch = qaoa.QaoaBatch([insts[i] for i in mine], 4, prec)
         tuned = batch.autotune()  # the schedule shape (cluster size), chosen by timing
         batch.run()
         times = []
         for _ in range(max(3, args.steps // 5)):
+            barrier(dist)
             t0 = time.perf_counter()
             e = batch.run()
-            times.append(time.perf_counter() - t0)
-        amps = batch.amplitudes
+            times.append(max_over_ranks(dist, time.perf_counter() - t0))
+        amps = sum(1 << insts[i]["n"] for i in range(len(insts)))
+        energies = replicas.gather_values(dist, mine, e, len(insts), device="cuda")
         out[prec] = {"cluster": batch.cluster, "autotune_seconds": tuned, "seconds_per_launch": statistics.median(times),
                      "instances_per_s": len(insts) / statistics.median(times),
-                     "amplitude_layers_per_s": amps * 4 / statistics.median(times), "energies": e}
+                     "amplitude_layers_per_s": amps * 4 / statistics.median(times), "energies": energies}
         batch.close()
+    if rank != 0:
+        if dist is not None:
+            dist.destroy_process_group()
+        return
     # exact <H> of a few instances from the CPU oracle
     import ctypes as C
     lib = B.oracle()
@@ -504,8 +509,10 @@ def run_qaoa(args):
                             f"seed {args.seed}", "amplitudes": int(sum(1 << x["n"] for x in insts))},
             "fp64": {k: v for k, v in out["fp64"].items() if k != "energies"},
             "fp32": {k: v for k, v in out["fp32"].items() if k != "energies"},
-            "max_abs_energy_error_vs_oracle": errs, "data": "synthetic"}
+            "max_abs_energy_error_vs_oracle": errs, "n_gpus": world, "scaling": "strong", "data": "synthetic"}
     print(json.dumps(line))
+    if dist is not None:
+        dist.destroy_process_group()
 
 
 def run_learned(args):
