@@ -501,19 +501,34 @@ __global__ void __launch_bounds__(kTileThreads, 1) k_tile_tc(float2* __restrict_
 	constexpr uint32_t kAmps = 1u << kTcTileQubits;
 	constexpr int kBatch = kAmps / kTileThreads;  // 8 loads in flight per thread
 	uint32_t mma_phase = 0;
-	for (uint64_t tile = blockIdx.x; tile < ntiles && !stop; tile += gridDim.x) {
+	auto tile_base = [&](uint64_t tile) {
 		uint64_t base = 0;
 		for (int j = 0; j < p.nfixed; ++j)
 			if ((tile >> j) & 1ULL) base |= 1ULL << p.fixed[j];
-		{
-			float2 r[kBatch];
+		return base;
+	};
+	// the next tile's amplitudes are loaded into registers while the current tile is processed
+	float2 pre[kBatch];
+	if (blockIdx.x < ntiles) {
+		const uint64_t b0 = tile_base(blockIdx.x);
+#pragma unroll
+		for (int b = 0; b < kBatch; ++b) {
+			const uint32_t j = threadIdx.x + b * kTileThreads;
+			pre[b] = s[b0 | highoff[j >> p.L] | (j & lowmask)];
+		}
+	}
+	for (uint64_t tile = blockIdx.x; tile < ntiles && !stop; tile += gridDim.x) {
+		const uint64_t base = tile_base(tile);
+#pragma unroll
+		for (int b = 0; b < kBatch; ++b) sm[threadIdx.x + b * kTileThreads] = pre[b];
+		const uint64_t next = tile + gridDim.x;
+		if (next < ntiles) {
+			const uint64_t nb = tile_base(next);
 #pragma unroll
 			for (int b = 0; b < kBatch; ++b) {
 				const uint32_t j = threadIdx.x + b * kTileThreads;
-				r[b] = s[base | highoff[j >> p.L] | (j & lowmask)];
+				pre[b] = s[nb | highoff[j >> p.L] | (j & lowmask)];
 			}
-#pragma unroll
-			for (int b = 0; b < kBatch; ++b) sm[threadIdx.x + b * kTileThreads] = r[b];
 		}
 		__syncthreads();
 		for (uint32_t oi = 0; oi < p.op_count; ++oi) {
