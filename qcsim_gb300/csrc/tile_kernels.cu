@@ -2,6 +2,7 @@
 // every gate of the pass with the same per-amplitude arithmetic as the per-gate kernels (gate_math.cuh),
 // and writes the tile back.  A persistent grid walks the 2^(n-k) tiles.
 #include <algorithm>
+#include <mutex>
 
 #include "gate_math.cuh"
 #include "tcgen05.cuh"
@@ -192,6 +193,58 @@ __device__ __forceinline__ void tile_phaserow(cplx_t<T>* sm, uint32_t items, con
 	}
 }
 
+// small fused FP32 blocks: each thread holds IPT items' inputs in registers, so that every matrix
+// entry loaded serves IPT items (the matrix loads, not the FMAs, bound the one-item form)
+template <typename T, int K, int IPT>
+__device__ __forceinline__ void tile_denseN_multi(cplx_t<T>* sm, uint32_t items, const OpRegs op, const cplx_t<T>* __restrict__ mats) {
+	constexpr int D = 1 << K;
+	uint32_t bits[K];
+#pragma unroll
+	for (int j = 0; j < K; ++j) bits[j] = 1u << static_cast<uint32_t>((op.ins >> (8 * j)) & 0xffu);
+	for (uint32_t i0 = threadIdx.x; i0 < items; i0 += blockDim.x * IPT) {
+		uint32_t b[IPT];
+		cplx_t<T> v[IPT][D];
+#pragma unroll
+		for (int it = 0; it < IPT; ++it) {
+			const uint32_t i = i0 + it * blockDim.x;
+			b[it] = expand_local(i < items ? i : i0, op);
+#pragma unroll
+			for (int c = 0; c < D; ++c) {
+				uint32_t x = b[it];
+#pragma unroll
+				for (int j = 0; j < K; ++j)
+					if ((c >> j) & 1) x |= bits[j];
+				v[it][c] = sm[x];
+			}
+		}
+#pragma unroll 1
+		for (int r = 0; r < D; ++r) {
+			const cplx_t<T>* row = mats + op.mat + r * D;
+			T re[IPT], im[IPT];
+#pragma unroll
+			for (int it = 0; it < IPT; ++it) re[it] = im[it] = 0;
+#pragma unroll
+			for (int c = 0; c < D; ++c) {
+				const cplx_t<T> mm = row[c];
+#pragma unroll
+				for (int it = 0; it < IPT; ++it) {
+					re[it] = fma(mm.x, v[it][c].x, re[it]);
+					re[it] = fma(-mm.y, v[it][c].y, re[it]);
+					im[it] = fma(mm.x, v[it][c].y, im[it]);
+					im[it] = fma(mm.y, v[it][c].x, im[it]);
+				}
+			}
+			uint32_t rb = 0;
+#pragma unroll
+			for (int j = 0; j < K; ++j)
+				if ((r >> j) & 1) rb |= bits[j];
+#pragma unroll
+			for (int it = 0; it < IPT; ++it)
+				if (i0 + it * blockDim.x < items) sm[b[it] | rb] = mk<T>(re[it], im[it]);
+		}
+	}
+}
+
 // DENSE: whether this instantiation carries the dense-block paths (they need many registers; passes
 // without dense blocks run the lighter instantiation at higher occupancy)
 template <typename T, bool DENSE>
@@ -255,9 +308,9 @@ __device__ __forceinline__ void tile_apply(cplx_t<T>* sm, int k, const TileOp& t
 	} else if constexpr (sizeof(T) == 4) {
 		// fused blocks (the FP32 path)
 		switch (op.nins) {
-		case 1: tile_denseN<T, 1>(sm, items, op, mats); break;
-		case 2: tile_denseN<T, 2>(sm, items, op, mats); break;
-		case 3: tile_denseN<T, 3>(sm, items, op, mats); break;
+		case 1: tile_denseN_multi<T, 1, 4>(sm, items, op, mats); break;
+		case 2: tile_denseN_multi<T, 2, 4>(sm, items, op, mats); break;
+		case 3: tile_denseN_multi<T, 3, 2>(sm, items, op, mats); break;
 		case 4: tile_denseN<T, 4>(sm, items, op, mats); break;
 		default: tile_denseN<T, 5>(sm, items, op, mats); break;
 		}
@@ -570,16 +623,33 @@ __global__ void __launch_bounds__(kTileThreads, 1) k_tile_tc(float2* __restrict_
 template <> int tile_qubits<double>() { return 12; }
 template <> int tile_qubits<float>() { return 13; }
 
+namespace {
+// kernel attributes and occupancies are per device: set up once per device (and per precision)
+constexpr int kMaxDevices = 64;
+std::mutex g_launch_mutex;
+
+cudaError_t current_device(int* dev) {
+	cudaError_t e = cudaGetDevice(dev);
+	if (e == cudaSuccess && (*dev < 0 || *dev >= kMaxDevices)) e = cudaErrorInvalidDevice;
+	return e;
+}
+}  // namespace
+
 template <typename T>
 cudaError_t launch_tile_pass(cplx_t<T>* s, const TilePass& p, const TileOp* d_ops, const cplx_t<T>* d_mats, int sms, cudaStream_t st,
                              int* d_err) {
+	int dev = 0;
+	if (cudaError_t e = current_device(&dev)) return e;
 	if constexpr (sizeof(T) == 4) {
 		if (p.dense == 2) {
-			static bool tc_configured = false;
-			if (!tc_configured) {
-				cudaError_t e = cudaFuncSetAttribute(k_tile_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(kTcSmem));
-				if (e != cudaSuccess) return e;
-				tc_configured = true;
+			static bool tc_configured[kMaxDevices] = {};
+			{
+				std::lock_guard<std::mutex> lock(g_launch_mutex);
+				if (!tc_configured[dev]) {
+					cudaError_t e = cudaFuncSetAttribute(k_tile_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(kTcSmem));
+					if (e != cudaSuccess) return e;
+					tc_configured[dev] = true;
+				}
 			}
 			if (p.k != kTcTileQubits || p.L < 5 || p.k - p.L > kMaxHigh || !d_err) return cudaErrorInvalidValue;
 			const uint64_t ntiles = 1ULL << p.nfixed;
@@ -594,18 +664,23 @@ cudaError_t launch_tile_pass(cplx_t<T>* s, const TilePass& p, const TileOp* d_op
 	constexpr int kDenseThreads = sizeof(T) == 4 ? 256 : kTileThreads;
 	auto* light = k_tile<T, false, kTileThreads>;
 	auto* dense = k_tile<T, true, kDenseThreads>;
-	static int per_sm[2] = {0, 0};
+	static int per_sm_dev[kMaxDevices][2] = {};
+	int* per_sm = per_sm_dev[dev];
 	const size_t smem = (size_t(1) << p.k) * sizeof(cplx_t<T>);
-	if (!per_sm[0]) {
-		const int maxs = static_cast<int>((size_t(1) << tile_qubits<T>()) * sizeof(cplx_t<T>));
-		cudaError_t e = cudaFuncSetAttribute(light, cudaFuncAttributeMaxDynamicSharedMemorySize, maxs);
-		if (e == cudaSuccess) e = cudaFuncSetAttribute(dense, cudaFuncAttributeMaxDynamicSharedMemorySize, maxs);
-		// resident CTAs per SM at the largest tile (registers and shared memory both counted)
-		if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm[0], light, kTileThreads, static_cast<size_t>(maxs));
-		if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm[1], dense, kDenseThreads, static_cast<size_t>(maxs));
-		if (e != cudaSuccess) return e;
-		per_sm[0] = std::max(per_sm[0], 1);
-		per_sm[1] = std::max(per_sm[1], 1);
+	{
+		std::lock_guard<std::mutex> lock(g_launch_mutex);
+		if (!per_sm[0]) {
+			const int maxs = static_cast<int>((size_t(1) << tile_qubits<T>()) * sizeof(cplx_t<T>));
+			int occ[2] = {0, 0};
+			cudaError_t e = cudaFuncSetAttribute(light, cudaFuncAttributeMaxDynamicSharedMemorySize, maxs);
+			if (e == cudaSuccess) e = cudaFuncSetAttribute(dense, cudaFuncAttributeMaxDynamicSharedMemorySize, maxs);
+			// resident CTAs per SM at the largest tile (registers and shared memory both counted)
+			if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ[0], light, kTileThreads, static_cast<size_t>(maxs));
+			if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ[1], dense, kDenseThreads, static_cast<size_t>(maxs));
+			if (e != cudaSuccess) return e;
+			per_sm[1] = std::max(occ[1], 1);
+			per_sm[0] = std::max(occ[0], 1);
+		}
 	}
 	if (p.k - p.L > kMaxHigh || p.k > tile_qubits<T>()) return cudaErrorInvalidValue;
 	const uint64_t ntiles = 1ULL << p.nfixed;
