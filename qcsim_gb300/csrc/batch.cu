@@ -588,11 +588,21 @@ std::vector<CompiledGate> qft_compiled(uint32_t start, uint32_t end, bool invers
 
 }  // namespace
 
+// the QFT always runs through the pass planner with phase rows (also on fused FP32 registers: its
+// controlled phases couple distant qubits, which dense blocks would spread over many passes)
 int qft_apply(qcs_handle h, uint32_t start, uint32_t end, bool inverse, bool do_swap) {
 	const std::vector<qcs_gate> gs = qft_gates(start, end, inverse, do_swap);
-	const int fusion = h->fusion >= 0 ? h->fusion : (h->prec == QCS_FP32 ? 1 : 0);
 	const int kmax = h->prec == QCS_FP64 ? tile_qubits<double>() : tile_qubits<float>();
-	if (fusion > 0 || per_gate_mode(h, gs.size(), kmax)) return batch_apply(h, gs.data(), gs.size());
+	if (per_gate_mode(h, gs.size(), kmax)) {
+		for (const qcs_gate& g : gs) {
+			cudaError_t e = apply_one(h, g);
+			if (e != cudaSuccess) {
+				h->err = std::string("qft: ") + cudaGetErrorString(e);
+				return QCS_CUDA_ERROR;
+			}
+		}
+		return QCS_OK;
+	}
 	return plan_and_run(h, qft_compiled(start, end, inverse, do_swap), kmax);
 }
 

@@ -367,21 +367,24 @@ def test_qft_passes(Q):
     assert np.abs(got - oracle_state(n, circuits.qft_circuit(0, n - 1), v)).max() <= TOL
 
 
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
 @pytest.mark.parametrize("start,end", [(0, 17), (2, 15), (1, 17), (0, 8), (9, 17)])
-def test_qft_phase_rows(Q, start, end):
+def test_qft_phase_rows(Q, start, end, precision):
     """QFT / IQFT on a sub-register of an 18-qubit register (shared-memory passes, each target's run of
-    controlled phases applied as one row) against the oracle's gate-by-gate sequence"""
+    controlled phases applied as one row; FP32 registers too, whose gate lists are otherwise fused)
+    against the oracle's gate-by-gate sequence"""
     from qcsim_gb300 import algorithms, circuits
     n = 18
+    tol = TOL if precision == "fp64" else 2e-6
     v = circuits.random_normal_state(n, 21 + start + end)
     for inverse in (False, True):
         for do_swap in (False, True):
-            reg = Q.QubitRegister(n, seed=1)
+            reg = Q.QubitRegister(n, seed=1, precision=precision)
             reg.setRegisterStorageFastNoNormalize(v)
             qft = algorithms.QuantumFourierTransform(n, start, end)
             (qft.IQFT if inverse else qft.QFT)(reg, do_swap)
             want = oracle_state(n, circuits.qft_circuit(start, end, inverse=inverse, do_swap=do_swap), v)
-            assert np.abs(reg.getRegisterStorage() - want).max() <= TOL, (inverse, do_swap)
+            assert np.abs(reg.getRegisterStorage() - want).max() <= tol, (inverse, do_swap)
 
 
 @pytest.mark.parametrize("n,max_q", [(10, 5), (16, 5), (18, 3), (20, 4)])
@@ -440,6 +443,30 @@ def test_fused_fp64(Q):
     reg.set_fusion(1, 4)
     reg.ApplyGates(ops)
     assert np.abs(reg.getRegisterStorage() - oracle_state(n, ops)).max() <= 1e-12
+
+
+@pytest.mark.parametrize("n,precision,depth", [(30, "fp64", 3), (33, "fp32", 2)])
+def test_full_size_round_trips(Q, n, precision, depth):
+    """the configurations' full sizes (30 qubits FP64 = 16 GiB; 33 qubits FP32 = 64 GiB, fused path with
+    tensor-core blocks) through size-independent properties: QFT|0> is the uniform state, a layered
+    circuit followed by its inverse and the inverse QFT return |0>"""
+    from qcsim_gb300 import algorithms, circuits
+    tol = 1e-10 if precision == "fp64" else 2e-4
+    reg = Q.QubitRegister(n, seed=1, precision=precision)
+    qft = algorithms.QuantumFourierTransform(n)
+    qft.QFT(reg)
+    u = 2.0 ** (-n / 2)
+    for idx in (0, 1, (1 << n) - 1, 0x2AAAAAAA & ((1 << n) - 1)):
+        assert abs(reg.getBasisStateAmplitude(idx) - u) < tol * u * 50
+    for q in (0, n // 2, n - 1):
+        assert abs(reg.GetQubitProbability(q) - 0.5) < tol
+    ops = circuits.layered_circuit(n, depth, seed=77, p3=0.05)
+    reg.ApplyGates(ops)
+    inv = [(type(g)(*(-x for x in g.params()[:1])) if hasattr(g, "theta") else g, *q) for (g, *q) in reversed(ops)]
+    reg.ApplyGates(inv)
+    qft.IQFT(reg)
+    assert abs(reg.getBasisStateAmplitude(0) - 1) < tol
+    reg.close()
 
 
 def test_larger_register_properties(Q):
