@@ -245,6 +245,25 @@ __device__ __forceinline__ void tile_denseN_multi(cplx_t<T>* sm, uint32_t items,
 	}
 }
 
+// tile index -> the global bits of its non-tile qubits: three 256-entry tables over the index's bytes
+// (a tile index has at most 24 bits: registers of at most 36 qubits, tiles of at least 12), built
+// once per CTA so that a tile's base costs three shared-memory loads
+constexpr int kFixChunks = 3;
+__device__ __forceinline__ void build_fix_tables(uint64_t (*fixtab)[256], const TilePass& p) {
+	for (uint32_t i = threadIdx.x; i < kFixChunks * 256; i += blockDim.x) {
+		const uint32_t c = i >> 8, v = i & 255u;
+		uint64_t off = 0;
+		for (int b = 0; b < 8; ++b) {
+			const int j = static_cast<int>(8 * c) + b;
+			if (j < p.nfixed && ((v >> b) & 1u)) off |= 1ULL << p.fixed[j];
+		}
+		fixtab[c][v] = off;
+	}
+}
+__device__ __forceinline__ uint64_t fixed_base(const uint64_t (*fixtab)[256], uint64_t tile) {
+	return fixtab[0][tile & 255u] | fixtab[1][(tile >> 8) & 255u] | fixtab[2][(tile >> 16) & 255u];
+}
+
 // DENSE: whether this instantiation carries the dense-block paths (they need many registers; passes
 // without dense blocks run the lighter instantiation at higher occupancy)
 template <typename T, bool DENSE>
@@ -329,8 +348,10 @@ __global__ void __launch_bounds__(THREADS) k_tile(cplx_t<T>* __restrict__ s, Til
                                                  const cplx_t<T>* __restrict__ mats, uint64_t ntiles) {
 	extern __shared__ __align__(1024) unsigned char smraw[];
 	__shared__ uint64_t highoff[1 << kMaxHigh];
+	__shared__ uint64_t fixtab[kFixChunks][256];
 	cplx_t<T>* sm = reinterpret_cast<cplx_t<T>*>(smraw);
 	const uint32_t K = 1u << p.k;
+	build_fix_tables(fixtab, p);
 	const uint32_t lowmask = (1u << p.L) - 1;
 	const int nh = p.k - p.L;
 	for (uint32_t h = threadIdx.x; h < (1u << nh); h += blockDim.x) {
@@ -341,9 +362,7 @@ __global__ void __launch_bounds__(THREADS) k_tile(cplx_t<T>* __restrict__ s, Til
 	}
 	__syncthreads();
 	for (uint64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-		uint64_t base = 0;
-		for (int j = 0; j < p.nfixed; ++j)
-			if ((tile >> j) & 1ULL) base |= 1ULL << p.fixed[j];
+		const uint64_t base = fixed_base(fixtab, tile);
 		// loads in batches of load_batch per thread, all issued before the first shared-memory store
 		for (uint32_t j0 = threadIdx.x; j0 < K; j0 += blockDim.x * load_batch<T>()) {
 			cplx_t<T> r[load_batch<T>()];
@@ -396,7 +415,8 @@ __global__ void __launch_bounds__(THREADS) k_tile(cplx_t<T>* __restrict__ s, Til
 constexpr uint32_t kTcTileBytes = (1u << kTcTileQubits) * sizeof(float2);
 constexpr uint32_t kTcLboA = 144;     // A operand: a row's core matrices fall in different bank groups
 constexpr uint32_t kTcABytes = 36864;  // one split of A: 16 row groups x 16 core matrices x 144 bytes
-constexpr uint32_t kTcSmem = kTcTileBytes + 2 * kTcABytes + kTcMatBudget;
+constexpr uint32_t kTcSmem = kTcTileBytes + 2 * kTcABytes + kTcMatBudget;  // plus the pass's operations
+constexpr uint32_t kTcSmemLimit = 216 * 1024;                                 // dynamic, with 9 KB static beside it
 constexpr uint32_t kTcTmemCols = 64;
 constexpr uint32_t kTcWaitTries = 1u << 22;
 
@@ -517,12 +537,17 @@ __global__ void __launch_bounds__(kTileThreads, 1) k_tile_tc(float2* __restrict_
                                                               const float2* __restrict__ mats, uint64_t ntiles, int* err) {
 	extern __shared__ __align__(1024) unsigned char smraw[];
 	__shared__ uint64_t highoff[1 << kMaxHigh];
+	__shared__ uint64_t fixtab[kFixChunks][256];
 	__shared__ __align__(8) uint64_t mbar_mma;
 	__shared__ uint32_t tmem_slot;
 	__shared__ int stop;
 	float2* sm = reinterpret_cast<float2*>(smraw);
 	unsigned char* sA = smraw + kTcTileBytes;
 	unsigned char* sB = sA + 2 * kTcABytes;
+	// the pass's operations, copied once (behind the block matrices)
+	TileOp* sops = reinterpret_cast<TileOp*>(sB + kTcMatBudget);
+	for (uint32_t i = threadIdx.x; i < p.op_count; i += blockDim.x) sops[i] = ops[p.op_begin + i];
+	build_fix_tables(fixtab, p);
 	const uint32_t warp = threadIdx.x >> 5;
 	const uint32_t lowmask = (1u << p.L) - 1;
 	const int nh = p.k - p.L;
@@ -554,12 +579,7 @@ __global__ void __launch_bounds__(kTileThreads, 1) k_tile_tc(float2* __restrict_
 	constexpr uint32_t kAmps = 1u << kTcTileQubits;
 	constexpr int kBatch = kAmps / kTileThreads;  // 8 loads in flight per thread
 	uint32_t mma_phase = 0;
-	auto tile_base = [&](uint64_t tile) {
-		uint64_t base = 0;
-		for (int j = 0; j < p.nfixed; ++j)
-			if ((tile >> j) & 1ULL) base |= 1ULL << p.fixed[j];
-		return base;
-	};
+	auto tile_base = [&](uint64_t tile) { return fixed_base(fixtab, tile); };
 	// the next tile's amplitudes are loaded into registers while the current tile is processed
 	float2 pre[kBatch];
 	if (blockIdx.x < ntiles) {
@@ -585,7 +605,7 @@ __global__ void __launch_bounds__(kTileThreads, 1) k_tile_tc(float2* __restrict_
 		}
 		__syncthreads();
 		for (uint32_t oi = 0; oi < p.op_count; ++oi) {
-			const TileOp op = ops[p.op_begin + oi];
+			const TileOp op = sops[oi];
 			if ((base & op.gmask) != op.gmask) continue;
 			if (static_cast<TKind>(op.kind) == TKind::DenseTC) {
 				const bool ok = op.nins == 5 ? tile_block_tc<5>(sm, op.ins, sA, sB + op.lbit1, tmem, &mbar_mma, mma_phase)
@@ -646,15 +666,18 @@ cudaError_t launch_tile_pass(cplx_t<T>* s, const TilePass& p, const TileOp* d_op
 			{
 				std::lock_guard<std::mutex> lock(g_launch_mutex);
 				if (!tc_configured[dev]) {
-					cudaError_t e = cudaFuncSetAttribute(k_tile_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(kTcSmem));
+					cudaError_t e = cudaFuncSetAttribute(k_tile_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(kTcSmemLimit));
 					if (e != cudaSuccess) return e;
 					tc_configured[dev] = true;
 				}
 			}
-			if (p.k != kTcTileQubits || p.L < 5 || p.k - p.L > kMaxHigh || !d_err) return cudaErrorInvalidValue;
+			const size_t smem = kTcSmem + static_cast<size_t>(p.op_count) * sizeof(TileOp);
+			if (p.k != kTcTileQubits || p.L < 5 || p.k - p.L > kMaxHigh || p.nfixed > 8 * kFixChunks || !d_err ||
+			    smem > kTcSmemLimit)
+				return cudaErrorInvalidValue;
 			const uint64_t ntiles = 1ULL << p.nfixed;
 			const uint64_t grid = std::min<uint64_t>(static_cast<uint64_t>(sms), ntiles);
-			k_tile_tc<<<static_cast<unsigned>(grid), kTileThreads, kTcSmem, st>>>(s, p, d_ops, d_mats, ntiles, d_err);
+			k_tile_tc<<<static_cast<unsigned>(grid), kTileThreads, smem, st>>>(s, p, d_ops, d_mats, ntiles, d_err);
 			note_launches(1);
 			return cudaGetLastError();
 		}
@@ -682,7 +705,7 @@ cudaError_t launch_tile_pass(cplx_t<T>* s, const TilePass& p, const TileOp* d_op
 			per_sm[0] = std::max(occ[0], 1);
 		}
 	}
-	if (p.k - p.L > kMaxHigh || p.k > tile_qubits<T>()) return cudaErrorInvalidValue;
+	if (p.k - p.L > kMaxHigh || p.k > tile_qubits<T>() || p.nfixed > 8 * kFixChunks) return cudaErrorInvalidValue;
 	const uint64_t ntiles = 1ULL << p.nfixed;
 	const uint64_t grid = std::min<uint64_t>(static_cast<uint64_t>(sms) * per_sm[p.dense ? 1 : 0], ntiles);
 	if (p.dense) dense<<<static_cast<unsigned>(grid), kDenseThreads, smem, st>>>(s, p, d_ops, d_mats, ntiles);
