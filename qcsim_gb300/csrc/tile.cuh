@@ -47,6 +47,7 @@ struct TilePass {
 	uint8_t fixed[40];     // global positions of the non-tile qubits, ascending
 	uint32_t op_begin, op_count;
 	int dense;             // 0: light operations only; 1: dense blocks on the CUDA cores; 2: tensor-core blocks
+	int ops_in_smem;       // set by the launcher: the CTA copies the pass's operations into shared memory
 };
 
 // d_err: set non-zero by a tensor-core pass whose bounded waits ran out (1: MMA completion, 2: tile load)

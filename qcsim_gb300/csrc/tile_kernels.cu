@@ -352,6 +352,13 @@ __global__ void __launch_bounds__(THREADS) k_tile(cplx_t<T>* __restrict__ s, Til
 	cplx_t<T>* sm = reinterpret_cast<cplx_t<T>*>(smraw);
 	const uint32_t K = 1u << p.k;
 	build_fix_tables(fixtab, p);
+	// the pass's operations: from shared memory (behind the tile) when the launcher left room for them
+	const TileOp* opsrc = ops + p.op_begin;
+	if (p.ops_in_smem) {
+		TileOp* sops = reinterpret_cast<TileOp*>(smraw + static_cast<size_t>(K) * sizeof(cplx_t<T>));
+		for (uint32_t i = threadIdx.x; i < p.op_count; i += blockDim.x) sops[i] = ops[p.op_begin + i];
+		opsrc = sops;
+	}
 	const uint32_t lowmask = (1u << p.L) - 1;
 	const int nh = p.k - p.L;
 	for (uint32_t h = threadIdx.x; h < (1u << nh); h += blockDim.x) {
@@ -379,7 +386,7 @@ __global__ void __launch_bounds__(THREADS) k_tile(cplx_t<T>* __restrict__ s, Til
 		}
 		__syncthreads();
 		for (uint32_t oi = 0; oi < p.op_count; ++oi) {
-			const TileOp op = ops[p.op_begin + oi];
+			const TileOp op = opsrc[oi];
 			if ((base & op.gmask) != op.gmask) continue;
 			tile_apply<T, DENSE>(sm, p.k, op, mats, base, highoff, p.L);
 			__syncthreads();
@@ -655,6 +662,11 @@ cudaError_t current_device(int* dev) {
 }
 }  // namespace
 
+// largest dynamic shared memory of a pass CTA: the largest tile plus room for its operations
+template <typename T> constexpr int maxs_of() {
+	return static_cast<int>((size_t(1) << (sizeof(T) == 4 ? 13 : 12)) * sizeof(cplx_t<T>)) + 48 * 1024;
+}
+
 template <typename T>
 cudaError_t launch_tile_pass(cplx_t<T>* s, const TilePass& p, const TileOp* d_ops, const cplx_t<T>* d_mats, int sms, cudaStream_t st,
                              int* d_err) {
@@ -695,8 +707,8 @@ cudaError_t launch_tile_pass(cplx_t<T>* s, const TilePass& p, const TileOp* d_op
 		if (!per_sm[0]) {
 			const int maxs = static_cast<int>((size_t(1) << tile_qubits<T>()) * sizeof(cplx_t<T>));
 			int occ[2] = {0, 0};
-			cudaError_t e = cudaFuncSetAttribute(light, cudaFuncAttributeMaxDynamicSharedMemorySize, maxs);
-			if (e == cudaSuccess) e = cudaFuncSetAttribute(dense, cudaFuncAttributeMaxDynamicSharedMemorySize, maxs);
+			cudaError_t e = cudaFuncSetAttribute(light, cudaFuncAttributeMaxDynamicSharedMemorySize, maxs_of<T>());
+			if (e == cudaSuccess) e = cudaFuncSetAttribute(dense, cudaFuncAttributeMaxDynamicSharedMemorySize, maxs_of<T>());
 			// resident CTAs per SM at the largest tile (registers and shared memory both counted)
 			if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ[0], light, kTileThreads, static_cast<size_t>(maxs));
 			if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ[1], dense, kDenseThreads, static_cast<size_t>(maxs));
@@ -707,9 +719,17 @@ cudaError_t launch_tile_pass(cplx_t<T>* s, const TilePass& p, const TileOp* d_op
 	}
 	if (p.k - p.L > kMaxHigh || p.k > tile_qubits<T>() || p.nfixed > 8 * kFixChunks) return cudaErrorInvalidValue;
 	const uint64_t ntiles = 1ULL << p.nfixed;
-	const uint64_t grid = std::min<uint64_t>(static_cast<uint64_t>(sms) * per_sm[p.dense ? 1 : 0], ntiles);
-	if (p.dense) dense<<<static_cast<unsigned>(grid), kDenseThreads, smem, st>>>(s, p, d_ops, d_mats, ntiles);
-	else light<<<static_cast<unsigned>(grid), kTileThreads, smem, st>>>(s, p, d_ops, d_mats, ntiles);
+	const int resident = per_sm[p.dense ? 1 : 0];
+	const uint64_t grid = std::min<uint64_t>(static_cast<uint64_t>(sms) * resident, ntiles);
+	// stage the operations in shared memory when that keeps the same number of CTAs per SM (228 KB per
+	// SM, 1 KB reserved per CTA, 9 KB static per CTA)
+	TilePass q = p;
+	const size_t ops_bytes = static_cast<size_t>(p.op_count) * sizeof(TileOp);
+	const size_t per_cta = (size_t(228) * 1024) / static_cast<size_t>(resident);
+	q.ops_in_smem = smem + ops_bytes + 10 * 1024 <= per_cta && smem + ops_bytes <= static_cast<size_t>(maxs_of<T>()) ? 1 : 0;
+	const size_t dyn = smem + (q.ops_in_smem ? ops_bytes : 0);
+	if (p.dense) dense<<<static_cast<unsigned>(grid), kDenseThreads, dyn, st>>>(s, q, d_ops, d_mats, ntiles);
+	else light<<<static_cast<unsigned>(grid), kTileThreads, dyn, st>>>(s, q, d_ops, d_mats, ntiles);
 	note_launches(1);
 	return cudaGetLastError();
 }
