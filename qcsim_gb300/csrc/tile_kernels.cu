@@ -467,7 +467,10 @@ template <int K> struct BlockBits {
 	}
 };
 
-// applies one DenseTC op of K qubits to the tile; false when the MMA completion wait ran out
+// applies one DenseTC op of K qubits to the tile; false when the MMA completion wait ran out.
+// Every index map of the op (tile index -> A-operand byte offset, tile index -> staging slot) is a sum
+// of one weight per set tile bit, so a thread's eight elements (tile index = thread + 512 b) cost one
+// 9-term sum for the thread's bits and three weights for b.
 template <int K>
 __device__ bool tile_block_tc(float2* sm, uint64_t ins, unsigned char* sA, const unsigned char* sBop, uint32_t tmem, uint64_t* mbar,
                               uint32_t& phase) {
@@ -475,14 +478,41 @@ __device__ bool tile_block_tc(float2* sm, uint64_t ins, unsigned char* sA, const
 	constexpr uint32_t sbo_a = (kdim / 4) * kTcLboA, sbo_b = (kdim / 4) * 128;
 	constexpr uint32_t cols = (1u << kTcTileQubits) >> K;  // 128 (K = 5) or 256 (K = 4)
 	constexpr uint32_t mt_bytes = 16 * sbo_a;                // one 128-row M tile of one split
+	constexpr uint32_t kTidBits = 9;                          // kTileThreads = 2^9
+	static_assert(kTileThreads == (1 << kTidBits) && kTcTileQubits == kTidBits + 3, "tile index = thread + 512 b");
 	const BlockBits<K> bb(ins);
+	// per tile bit: byte offset in one A split (a block bit is bit t of j, the K index is 2j + part; a
+	// column bit is bit r of the column: rows within a core matrix, row groups, then the M tile) and
+	// slot in the staging area (slot = j (cols + 1) + column)
+	uint32_t wa[kTcTileQubits], ws[kTcTileQubits];
+	{
+		uint32_t t = 0;
+#pragma unroll
+		for (uint32_t i = 0; i < kTcTileQubits; ++i) {
+			if (t < K && bb.pos[t == K ? 0 : t] == i) {
+				wa[i] = t == 0 ? 8u : (kTcLboA << (t - 1));
+				ws[i] = (cols + 1) << t;
+				++t;
+			} else {
+				const uint32_t r = i - t;
+				wa[i] = r < 3 ? (16u << r) : (r < 7 ? (sbo_a << (r - 3)) : mt_bytes);
+				ws[i] = 1u << r;
+			}
+		}
+	}
+	uint32_t a_tid = 0, s_tid = 0;
+#pragma unroll
+	for (uint32_t i = 0; i < kTidBits; ++i)
+		if ((threadIdx.x >> i) & 1u) {
+			a_tid += wa[i];
+			s_tid += ws[i];
+		}
 	// gather in tile order (conflict-free reads) into the A operand, split into TF32 hi and lo
-#pragma unroll 4
-	for (uint32_t x = threadIdx.x; x < (1u << kTcTileQubits); x += kTileThreads) {
-		const float2 v = sm[x];
-		const uint32_t c = bb.column(x), j = bb.index(x);
+#pragma unroll
+	for (uint32_t b = 0; b < 8; ++b) {
+		const float2 v = sm[threadIdx.x + (b << kTidBits)];
+		const uint32_t off = a_tid + ((b & 1u) ? wa[9] : 0u) + ((b & 2u) ? wa[10] : 0u) + ((b & 4u) ? wa[11] : 0u);
 		const float hx = tf32_rna(v.x), hy = tf32_rna(v.y);
-		const uint32_t off = (c >> 7) * mt_bytes + tc::kmajor_offset(c & 127u, 2 * j, kdim, kTcLboA);
 		*reinterpret_cast<float2*>(sA + off) = make_float2(hx, hy);
 		*reinterpret_cast<float2*>(sA + kTcABytes + off) = make_float2(tf32_rna(v.x - hx), tf32_rna(v.y - hy));
 	}
@@ -512,19 +542,22 @@ __device__ bool tile_block_tc(float2* sm, uint64_t ins, unsigned char* sA, const
 	phase ^= 1u;
 	tc::fence_after_sync();
 	// warp w reads tensor-memory lanes 32 (w % 4) + 0..31 (M-tile rows = columns) and the 16
-	// accumulator columns 16 (w / 4) + 0..15 (8 complex outputs)
+	// accumulator columns 16 (w / 4) + 0..15 (8 complex outputs i0..i0 + 7)
 	const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
 	const uint32_t quad = warp & 3u, cc = warp >> 2;
 	float v[16];
 	tc::tmem_ld16(tmem + ((32u * quad) << 16) + 16u * cc, v);
-	const uint32_t mt = (16u * cc) / kdim, i0 = ((16u * cc) % kdim) / 2;
+	const uint32_t mt = (16u * cc) / kdim, i0 = ((16u * cc) % kdim) / 2;  // i0: a multiple of 8
 	const uint32_t c = mt * 128u + 32u * quad + lane;
 	// blocks on three or more of the five lowest tile bits: outputs go through a padded staging area
 	// (the A operand is free now) and back to the tile in tile order; otherwise straight to the tile
 	const bool staged = bb.low_count() >= 3;
 	if (!staged) {
+		const uint32_t x0 = bb.place(c, i0);
+		const uint32_t p0 = 1u << bb.pos[0], p1 = 1u << bb.pos[1], p2 = 1u << bb.pos[2];
 #pragma unroll
-		for (uint32_t t = 0; t < 8; ++t) sm[bb.place(c, i0 + t)] = make_float2(v[2 * t], v[2 * t + 1]);
+		for (uint32_t t = 0; t < 8; ++t)
+			sm[x0 + ((t & 1u) ? p0 : 0u) + ((t & 2u) ? p1 : 0u) + ((t & 4u) ? p2 : 0u)] = make_float2(v[2 * t], v[2 * t + 1]);
 	} else {
 		float2* stage = reinterpret_cast<float2*>(sA);
 #pragma unroll
@@ -534,8 +567,9 @@ __device__ bool tile_block_tc(float2* sm, uint64_t ins, unsigned char* sA, const
 	if (staged) {
 		__syncthreads();
 		const float2* stage = reinterpret_cast<const float2*>(sA);
-#pragma unroll 4
-		for (uint32_t x = threadIdx.x; x < (1u << kTcTileQubits); x += kTileThreads) sm[x] = stage[bb.index(x) * (cols + 1) + bb.column(x)];
+#pragma unroll
+		for (uint32_t b = 0; b < 8; ++b)
+			sm[threadIdx.x + (b << kTidBits)] = stage[s_tid + ((b & 1u) ? ws[9] : 0u) + ((b & 2u) ? ws[10] : 0u) + ((b & 4u) ? ws[11] : 0u)];
 	}
 	return ok;
 }
