@@ -424,7 +424,7 @@ constexpr uint32_t kTcLboA = 144;     // A operand: a row's core matrices fall i
 constexpr uint32_t kTcABytes = 36864;  // one split of A: 16 row groups x 16 core matrices x 144 bytes
 constexpr uint32_t kTcSmem = kTcTileBytes + 2 * kTcABytes + kTcMatBudget;  // plus the pass's operations
 constexpr uint32_t kTcSmemLimit = 216 * 1024;                                 // dynamic, with 9 KB static beside it
-constexpr uint32_t kTcTmemCols = 64;
+constexpr uint32_t kTcTmemCols = 128;  // per M tile: kdim accumulator columns + kdim hi*lo columns
 constexpr uint32_t kTcWaitTries = 1u << 22;
 
 __device__ __forceinline__ float tf32_rna(float x) {
@@ -521,19 +521,20 @@ __device__ bool tile_block_tc(float2* sm, uint64_t ins, unsigned char* sA, const
 	__syncthreads();
 	tc::fence_after_sync();
 	if (threadIdx.x == 0) {
-		constexpr uint32_t idesc = tc::idesc_tf32(128, kdim);
+		constexpr uint32_t idesc = tc::idesc_tf32(128, kdim), idesc2 = tc::idesc_tf32(128, 2 * kdim);
 		const uint32_t a_hi = tc::smem_addr(sA), b_hi = tc::smem_addr(sBop);
 		// descriptors of k-step 0; each k-step advances the start address (16-byte units, low bits)
 		const uint64_t ah0 = tc::smem_desc(a_hi, kTcLboA, sbo_a), al0 = tc::smem_desc(a_hi + kTcABytes, kTcLboA, sbo_a);
-		const uint64_t bh0 = tc::smem_desc(b_hi, 128, sbo_b), bl0 = tc::smem_desc(b_hi + 16 * D * D, 128, sbo_b);
+		const uint64_t bh0 = tc::smem_desc(b_hi, 128, sbo_b);
 #pragma unroll
 		for (uint32_t mt = 0; mt < cols / 128; ++mt) {
 #pragma unroll
 			for (uint32_t ks = 0; ks < kdim / 8; ++ks) {
 				const uint64_t da = (mt * mt_bytes + ks * 2 * kTcLboA) >> 4, db = (ks * 2 * 128) >> 4;
-				tc::mma_tf32(tmem + mt * kdim, ah0 + da, bh0 + db, idesc, ks > 0 ? 1u : 0u);
-				tc::mma_tf32(tmem + mt * kdim, ah0 + da, bl0 + db, idesc, 1u);
-				tc::mma_tf32(tmem + mt * kdim, al0 + da, bh0 + db, idesc, 1u);
+				// B_lo directly follows B_hi: one N = 2 kdim product gives hi*hi in the first kdim columns
+				// and hi*lo in the next kdim; lo*hi accumulates onto the first
+				tc::mma_tf32(tmem + mt * 2 * kdim, ah0 + da, bh0 + db, idesc2, ks > 0 ? 1u : 0u);
+				tc::mma_tf32(tmem + mt * 2 * kdim, al0 + da, bh0 + db, idesc, 1u);
 			}
 		}
 		tc::mma_commit(mbar);
@@ -541,13 +542,17 @@ __device__ bool tile_block_tc(float2* sm, uint64_t ins, unsigned char* sA, const
 	const bool ok = tc::mbar_wait(mbar, phase, kTcWaitTries);
 	phase ^= 1u;
 	tc::fence_after_sync();
-	// warp w reads tensor-memory lanes 32 (w % 4) + 0..31 (M-tile rows = columns) and the 16
-	// accumulator columns 16 (w / 4) + 0..15 (8 complex outputs i0..i0 + 7)
+	// warp w reads tensor-memory lanes 32 (w % 4) + 0..31 (M-tile rows = columns), 16 accumulator
+	// columns (8 complex outputs i0..i0 + 7) and the matching 16 hi*lo columns kdim further on
 	const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
 	const uint32_t quad = warp & 3u, cc = warp >> 2;
-	float v[16];
-	tc::tmem_ld16(tmem + ((32u * quad) << 16) + 16u * cc, v);
-	const uint32_t mt = (16u * cc) / kdim, i0 = ((16u * cc) % kdim) / 2;  // i0: a multiple of 8
+	const uint32_t mt = (16u * cc) / kdim, within = (16u * cc) % kdim, i0 = within / 2;  // i0: a multiple of 8
+	float v[16], w[16];
+	const uint32_t tcol = tmem + ((32u * quad) << 16) + mt * 2 * kdim + within;
+	tc::tmem_ld16(tcol, v);
+	tc::tmem_ld16(tcol + kdim, w);
+#pragma unroll
+	for (int q = 0; q < 16; ++q) v[q] += w[q];
 	const uint32_t c = mt * 128u + 32u * quad + lane;
 	// blocks on three or more of the five lowest tile bits: outputs go through a padded staging area
 	// (the A operand is free now) and back to the tile in tile order; otherwise straight to the tile
