@@ -203,6 +203,11 @@ int qcs_block_features(uint32_t nqubits, const uint32_t* qubits, uint32_t k, uin
  * number of gates folded in; nblocks_out may exceed capacity (then only capacity entries are written) */
 int qcs_fusion_plan(uint32_t nqubits, const qcs_gate* gates, size_t count, int max_qubits, uint64_t* block_masks,
                     uint32_t* block_gates, size_t capacity, size_t* nblocks_out);
+/* the shared-memory passes the engine forms for that partition (host only, no GPU): tiles of
+ * `tile_qubits` qubits, the tensor-core matrix budget applied when tensor_cores != 0; pass_of_block[i]
+ * is block i's pass (blocks as numbered by qcs_fusion_plan, global-factor blocks get UINT32_MAX) */
+int qcs_fusion_passes(uint32_t nqubits, const qcs_gate* gates, size_t count, int max_qubits, int tile_qubits, int tensor_cores,
+                      uint32_t* pass_of_block, size_t capacity, size_t* nblocks_out, size_t* npasses_out);
 /* attach a trained model (kept by the caller) and the measured time of one pass per register size
  * (pass_ms[n], milliseconds); NULL detaches */
 int qcs_set_cost_model(qcs_handle h, qcs_mlp_handle mlp, const double* pass_ms, size_t len);

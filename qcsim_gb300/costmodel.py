@@ -52,6 +52,20 @@ def fusion_plan(n: int, recs: np.ndarray, max_qubits: int) -> list[tuple[int, in
     return [(int(masks[i]), int(ng[i])) for i in range(nb.value)]
 
 
+def fusion_passes(n: int, recs: np.ndarray, max_qubits: int, tile_qubits: int, tensor_cores: bool) -> list[int]:
+    """the shared-memory pass of each block of fusion_plan's partition (host only)"""
+    lib = L.load()
+    recs = np.ascontiguousarray(recs, dtype=L.GATE_DTYPE)
+    cap = len(recs) + 1
+    pob = np.zeros(cap, dtype=np.uint32)
+    nb, npass = C.c_size_t(), C.c_size_t()
+    L.check(lib.qcs_fusion_passes(n, recs.ctypes.data_as(C.c_void_p), len(recs), max_qubits, tile_qubits, int(tensor_cores),
+                                  pob.ctypes.data_as(C.POINTER(C.c_uint32)), cap, C.byref(nb), C.byref(npass)))
+    out = [int(x) for x in pob[:nb.value]]
+    assert not out or max(out) + 1 == npass.value
+    return out
+
+
 class Mlp:
     """the engine's MLP (qcs_mlp_*)"""
 

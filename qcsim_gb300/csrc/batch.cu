@@ -379,12 +379,6 @@ int run_planned(qcs_handle h, const std::vector<PlannedPass>& passes, int kmax, 
 
 }  // namespace
 
-// tile size of the fused path: tensor-core passes use tiles of kTcTileQubits
-int fused_tile_qubits(qcs_handle h) {
-	if (h->prec == QCS_FP64) return tile_qubits<double>();
-	return h->tensor_cores ? kTcTileQubits : tile_qubits<float>();
-}
-
 // dense blocks applied in shared-memory passes (the fused path and qcs_apply_matrix)
 int apply_blocks(qcs_handle h, std::vector<FusedBlock> blocks) {
 	const int n = static_cast<int>(h->n);
@@ -393,30 +387,26 @@ int apply_blocks(qcs_handle h, std::vector<FusedBlock> blocks) {
 	const bool tc = h->prec == QCS_FP32 && h->tensor_cores && big;
 	const int kmax = std::min(tc ? kTcTileQubits : (h->prec == QCS_FP64 ? tile_qubits<double>() : tile_qubits<float>()), n);
 	const int L0 = std::min(n, std::max(5, kmax - 8));
-	std::vector<PlannedPass> passes(1);
-	passes.back().tmask = (1ULL << L0) - 1;
-	uint32_t tc_bytes = 0;  // resident tensor-core matrices of the open pass
-	for (FusedBlock& b : blocks) {
-		if (b.qubits.empty()) {  // a global factor only
-			h->scale *= b.M[0];
-			continue;
+	for (const FusedBlock& b : blocks)
+		if (b.qubits.empty()) h->scale *= b.M[0];  // a global factor only
+	std::vector<PlannedPass> passes;
+	for (const std::vector<size_t>& ids : pack_blocks(blocks, kmax, L0, tc ? kTcMatBudget : 0u)) {
+		PlannedPass pp;
+		pp.tmask = (1ULL << L0) - 1;
+		for (size_t i : ids) {
+			CompiledGate c;
+			c.kind = GKind::Block;
+			c.block_q = blocks[i].qubits;
+			c.block_m = std::move(blocks[i].M);
+			c.block_gates = blocks[i].ngates;
+			pp.tmask |= c.local_mask();
+			pp.gates.push_back(std::move(c));
 		}
-		CompiledGate c;
-		c.kind = GKind::Block;
-		c.block_q = b.qubits;
-		c.block_m = std::move(b.M);
-		c.block_gates = b.ngates;
-		const uint64_t need = c.local_mask();
-		const uint32_t tcb = tc && c.block_q.size() >= 4 ? 32u << (2 * c.block_q.size()) : 0u;
-		if (popcount64(passes.back().tmask | need) > kmax || tc_bytes + tcb > kTcMatBudget) {
-			passes.emplace_back();
-			passes.back().tmask = ((1ULL << L0) - 1) | need;
-			tc_bytes = 0;
-		} else {
-			passes.back().tmask |= need;
-		}
-		tc_bytes += tcb;
-		passes.back().gates.push_back(std::move(c));
+		passes.push_back(std::move(pp));
+	}
+	if (passes.empty()) {
+		passes.emplace_back();
+		passes.back().tmask = (1ULL << L0) - 1;
 	}
 	h->last_blocks = blocks.size();
 	return h->prec == QCS_FP64 ? run_planned<double>(h, passes, kmax, L0) : run_planned<float>(h, passes, kmax, L0);
@@ -430,7 +420,8 @@ int fused_apply(qcs_handle h, const qcs_gate* gates, size_t count) {
 	for (size_t i = 0; i < count; ++i) cg.push_back(compile_gate(gates[i], false));
 	std::vector<FusedBlock> blocks;
 	if (h->fusion == 2 && h->cost_ctx) {
-		const int kmax = std::min(fused_tile_qubits(h), n);
+		// the non-tensor-core tile; candidates with tensor-core blocks use kTcTileQubits (costmodel.cu)
+		const int kmax = std::min(h->prec == QCS_FP64 ? tile_qubits<double>() : tile_qubits<float>(), n);
 		const int L0 = std::min(n, std::max(5, kmax - 8));
 		const int st = choose_partition(h, cg, kmax, L0, blocks, &h->last_predicted_ms);
 		if (st != QCS_OK) return st;

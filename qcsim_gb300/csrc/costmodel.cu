@@ -13,6 +13,7 @@
 #include "batch.cuh"
 #include "compile.cuh"
 #include "fusion.cuh"
+#include "tile.cuh"
 
 namespace qcs {
 
@@ -42,22 +43,9 @@ struct CostModel {
 	std::vector<double> pass_ms;  // index: register qubits
 };
 
-// passes the planner would form for these blocks (same packing rule as fused_apply)
-static int count_passes(const std::vector<FusedBlock>& blocks, int n, int kmax, int L0) {
-	int passes = 1;
-	uint64_t t = (1ULL << L0) - 1;
-	for (const FusedBlock& b : blocks) {
-		uint64_t need = 0;
-		for (uint32_t q : b.qubits) need |= 1ULL << q;
-		if (__builtin_popcountll(t | need) > kmax) {
-			++passes;
-			t = ((1ULL << L0) - 1) | need;
-		} else {
-			t |= need;
-		}
-	}
-	(void)n;
-	return passes;
+// passes the planner forms for these blocks (the packing of apply_blocks)
+static int count_passes(const std::vector<FusedBlock>& blocks, int kmax, int L0, bool tc) {
+	return static_cast<int>(pack_blocks(blocks, kmax, L0, tc ? kTcMatBudget : 0u).size());
 }
 
 int choose_partition(qcs_handle h, const std::vector<CompiledGate>& gates, int kmax, int L0, std::vector<FusedBlock>& best,
@@ -82,7 +70,10 @@ int choose_partition(qcs_handle h, const std::vector<CompiledGate>& gates, int k
 		double cost = 0;
 		for (float v : y) cost += std::exp(static_cast<double>(v));
 		const double pms = static_cast<size_t>(n) < cm->pass_ms.size() ? cm->pass_ms[static_cast<size_t>(n)] : 0.0;
-		cost += pms * count_passes(cand, n, kmax, L0);
+		bool big = false;
+		for (const FusedBlock& b : cand) big = big || b.qubits.size() >= 4;
+		const bool tc = h->prec == QCS_FP32 && h->tensor_cores && big;
+		cost += pms * count_passes(cand, tc ? std::min(kmax, kTcTileQubits) : kmax, L0, tc);
 		if (cost < best_cost) {
 			best_cost = cost;
 			best = std::move(cand);
@@ -134,6 +125,38 @@ int qcs_fusion_plan(uint32_t nqubits, const qcs_gate* gates, size_t count, int m
 		++k;
 	}
 	*nblocks_out = k;
+	return QCS_OK;
+}
+
+int qcs_fusion_passes(uint32_t nqubits, const qcs_gate* gates, size_t count, int max_qubits, int tile_qubits, int tensor_cores,
+                      uint32_t* pass_of_block, size_t capacity, size_t* nblocks_out, size_t* npasses_out) {
+	if ((!gates && count) || !nblocks_out || !npasses_out || max_qubits < 1 || max_qubits > 5 || tile_qubits < 5 || tile_qubits > 13)
+		return QCS_INVALID_ARGUMENT;
+	std::vector<qcs::CompiledGate> cg;
+	cg.reserve(count);
+	for (size_t i = 0; i < count; ++i) {
+		const qcs_gate& g = gates[i];
+		if (g.k < 1 || g.k > 3 || g.q0 >= nqubits || (g.k > 1 && g.q1 >= nqubits) || (g.k > 2 && g.q2 >= nqubits))
+			return QCS_INVALID_ARGUMENT;
+		cg.push_back(qcs::compile_gate(g, false));
+	}
+	qcs::FusionPolicy pol;
+	pol.max_qubits = max_qubits;
+	pol.nqubits = static_cast<int>(nqubits);
+	std::vector<qcs::FusedBlock> blocks = qcs::fuse(cg, pol);
+	// the numbering of qcs_fusion_plan: blocks with qubits only
+	std::vector<qcs::FusedBlock> real;
+	for (qcs::FusedBlock& b : blocks)
+		if (!b.qubits.empty()) real.push_back(std::move(b));
+	const int kmax = std::min(tile_qubits, static_cast<int>(nqubits));
+	const int L0 = std::min(static_cast<int>(nqubits), std::max(5, kmax - 8));
+	const auto passes = qcs::pack_blocks(real, kmax, L0, tensor_cores ? qcs::kTcMatBudget : 0u);
+	if (pass_of_block)
+		for (size_t p = 0; p < passes.size(); ++p)
+			for (size_t i : passes[p])
+				if (i < capacity) pass_of_block[i] = static_cast<uint32_t>(p);
+	*nblocks_out = real.size();
+	*npasses_out = passes.size();
 	return QCS_OK;
 }
 

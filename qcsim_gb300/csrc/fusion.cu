@@ -205,4 +205,42 @@ std::vector<FusedBlock> fuse(const std::vector<CompiledGate>& gates, const Fusio
 	return out;
 }
 
+std::vector<std::vector<size_t>> pack_blocks(const std::vector<FusedBlock>& blocks, int kmax, int L0, uint32_t tc_budget,
+                                             size_t window) {
+	std::vector<std::vector<size_t>> passes;
+	std::vector<char> placed(blocks.size(), 0);
+	std::vector<uint64_t> mask(blocks.size(), 0);
+	std::vector<uint32_t> tcb(blocks.size(), 0);
+	size_t first = 0;  // first block not yet placed
+	for (size_t i = 0; i < blocks.size(); ++i) {
+		for (uint32_t q : blocks[i].qubits) mask[i] |= 1ULL << q;
+		if (blocks[i].qubits.empty()) placed[i] = 1;
+		if (tc_budget && blocks[i].qubits.size() >= 4) tcb[i] = 32u << (2 * blocks[i].qubits.size());
+	}
+	const uint64_t low = (L0 >= 64) ? ~0ULL : ((1ULL << L0) - 1);
+	while (true) {
+		while (first < blocks.size() && placed[first]) ++first;
+		if (first == blocks.size()) break;
+		std::vector<size_t> pass;
+		uint64_t tmask = low, waiting = 0;
+		uint32_t bytes = 0;
+		size_t scanned = 0;
+		for (size_t i = first; i < blocks.size() && scanned < window; ++i) {
+			if (placed[i]) continue;
+			++scanned;
+			const bool fits = __builtin_popcountll(tmask | mask[i]) <= kmax && (!tc_budget || bytes + tcb[i] <= tc_budget);
+			if ((mask[i] & waiting) == 0 && (fits || pass.empty())) {
+				placed[i] = 1;
+				pass.push_back(i);
+				tmask |= mask[i];
+				bytes += tcb[i];
+			} else {
+				waiting |= mask[i];
+			}
+		}
+		passes.push_back(std::move(pass));
+	}
+	return passes;
+}
+
 }  // namespace qcs

@@ -30,6 +30,15 @@ struct FusionPolicy {
 // greedy fusion that reorders only gates on disjoint qubits (which commute)
 std::vector<FusedBlock> fuse(const std::vector<CompiledGate>& gates, const FusionPolicy& policy);
 
+// packs blocks into shared-memory passes of at most kmax tile qubits (qubits below L0 always in the
+// tile): each pass takes, in order, every block that fits and shares no qubit with an earlier block
+// still waiting (blocks on disjoint qubits commute), looking at most `window` blocks ahead.  With
+// tc_budget > 0, blocks of 4 and 5 qubits also draw 32 x 4^m bytes of resident matrices from that
+// budget.  Blocks without qubits (global factors) take no pass.  Returns the block indices of each
+// pass, each in the original order.
+std::vector<std::vector<size_t>> pack_blocks(const std::vector<FusedBlock>& blocks, int kmax, int L0, uint32_t tc_budget,
+                                             size_t window = 64);
+
 // apply one compiled gate (its effective operator, including its factored scale) to a vector over
 // the block's qubits, in block-local indexing
 void apply_compiled_local(const CompiledGate& c, const std::vector<uint32_t>& qubits, std::complex<double>* v);

@@ -154,6 +154,39 @@ def test_fusion_plan_covers_every_gate():
     assert counts == sorted(counts, reverse=True)
 
 
+def test_pass_packing_respects_order_and_tiles():
+    """the pass planner of the fused path (host code): every block lands in exactly one pass, a block
+    never runs before an earlier block it shares a qubit with, every pass fits its tile, and look-ahead
+    packing needs no more passes than packing strictly in order"""
+    if not L.LIB_PATH.exists():
+        pytest.skip("libqcs_gpu.so not built")
+    from qcsim_gb300 import costmodel
+    for n, mq, k, tc in ((26, 5, 12, True), (30, 3, 13, False), (24, 4, 12, True), (20, 2, 13, False)):
+        ops = circuits.layered_circuit(n, 8, seed=n + mq, p3=0.05, controlled_frac=0.1)
+        recs = G.records(ops)
+        plan = costmodel.fusion_plan(n, recs, mq)
+        passes = costmodel.fusion_passes(n, recs, mq, k, tc)
+        assert len(passes) == len(plan)
+        low = (1 << min(n, max(5, k - 8))) - 1
+        union: dict[int, int] = {}
+        for (mask, _), p in zip(plan, passes):
+            union[p] = union.get(p, low) | mask
+        assert sorted(union) == list(range(len(union)))
+        assert all(bin(m).count("1") <= k for m in union.values())
+        for i in range(len(plan)):
+            for j in range(i + 1, len(plan)):
+                if plan[i][0] & plan[j][0]:
+                    assert passes[i] <= passes[j], (i, j)
+        # strictly in order: a new pass whenever the next block does not fit
+        in_order, cur = 1, low
+        for mask, _ in plan:
+            if bin(cur | mask).count("1") > k:
+                in_order, cur = in_order + 1, low | mask
+            else:
+                cur |= mask
+        assert len(union) <= in_order
+
+
 def test_block_features_layout():
     if not L.LIB_PATH.exists():
         pytest.skip("libqcs_gpu.so not built")
