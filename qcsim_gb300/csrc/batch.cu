@@ -436,31 +436,55 @@ int fused_apply(qcs_handle h, const qcs_gate* gates, size_t count) {
 
 namespace {
 
-// packs compiled gates into shared-memory passes (greedy, in order) and runs them
+// packs compiled gates into shared-memory passes and runs them.  Each pass takes, in order, every gate
+// whose local qubits fit its tile and which shares no qubit with an earlier gate still waiting
+// (gates on disjoint qubits commute), looking at most kGateWindow gates ahead.  The global factors
+// taken out of the gates multiply into the register's scale in placement order; when its magnitude
+// leaves [1e-100, 1e100] the pass closes and the scale is folded into the amplitudes after it.
+constexpr size_t kGateWindow = 64;
+
 int plan_and_run(qcs_handle h, const std::vector<CompiledGate>& cg, int kmax) {
 	const int L0 = std::max(5, kmax - 8);
-	std::vector<PlannedPass> passes(1);
-	passes.back().tmask = (1ULL << L0) - 1;
-	for (const CompiledGate& c : cg) {
-		h->scale *= c.scale;
-		const double mag = std::abs(h->scale);
-		if (c.kind != GKind::Identity) {
-			const uint64_t need = c.local_mask();
-			PlannedPass& cur = passes.back();
-			if (popcount64(cur.tmask | need) > kmax) {
-				passes.emplace_back();
-				passes.back().tmask = ((1ULL << L0) - 1) | need;
+	const uint64_t low = (1ULL << L0) - 1;
+	std::vector<PlannedPass> passes;
+	std::vector<char> placed(cg.size(), 0);
+	size_t first = 0;
+	while (true) {
+		while (first < cg.size() && placed[first]) ++first;
+		if (first == cg.size()) break;
+		PlannedPass pp;
+		pp.tmask = low;
+		uint64_t waiting = 0;
+		size_t scanned = 0;
+		bool fold = false;
+		for (size_t i = first; i < cg.size() && scanned < kGateWindow && !fold; ++i) {
+			if (placed[i]) continue;
+			++scanned;
+			const CompiledGate& c = cg[i];
+			const uint64_t touch = c.touch_mask(), need = c.local_mask();
+			const bool fits = popcount64(pp.tmask | need) <= kmax;
+			if ((touch & waiting) == 0 && (fits || pp.gates.empty())) {
+				placed[i] = 1;
+				h->scale *= c.scale;
+				if (c.kind != GKind::Identity) {
+					pp.tmask |= need;
+					pp.gates.push_back(c);
+				}
+				const double mag = std::abs(h->scale);
+				if (mag > 1e100 || mag < 1e-100) {
+					pp.fold_after = h->scale;
+					h->scale = std::complex<double>(1.0, 0.0);
+					fold = true;
+				}
 			} else {
-				cur.tmask |= need;
+				waiting |= touch;
 			}
-			passes.back().gates.push_back(c);
 		}
-		if (mag > 1e100 || mag < 1e-100) {
-			passes.back().fold_after = h->scale;
-			h->scale = std::complex<double>(1.0, 0.0);
-			passes.emplace_back();
-			passes.back().tmask = (1ULL << L0) - 1;
-		}
+		passes.push_back(std::move(pp));
+	}
+	if (passes.empty()) {
+		passes.emplace_back();
+		passes.back().tmask = low;
 	}
 	return h->prec == QCS_FP64 ? run_planned<double>(h, passes, kmax, L0) : run_planned<float>(h, passes, kmax, L0);
 }
