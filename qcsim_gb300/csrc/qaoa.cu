@@ -100,19 +100,46 @@ struct TileGeo {
 };
 
 template <typename T>
+__device__ __forceinline__ void rx_pair(cplx_t<T>& a0, cplx_t<T>& a1, const Mat2<T>& m, int form) {
+	if (form == 0) op2<T, Op1::UnitIm01, 0>(a0, a1, m);
+	else op2<T, Op1::UnitIm10, 0>(a0, a1, m);
+}
+
+template <typename T>
 __device__ void rx_local(cplx_t<T>* sm, uint32_t k, uint32_t lo, uint32_t hi, const QLayer& L) {
-	// RX on local bits lo..hi-1 of a 2^k tile
+	// RX on local bits lo..hi-1 of a 2^k tile; in a two-bit sweep each item holds the four amplitudes
+	// of one (bit a, bit b) square and applies RX on a to both a-pairs, then on b
 	Mat2<T> m;
 	m.m00 = mk<T>(1, static_cast<T>(L.x0));
 	m.m01 = mk<T>(1, static_cast<T>(L.x1));
-	const uint32_t items = (1u << k) >> 1;
-	for (uint32_t b = lo; b < hi; ++b) {
+	uint32_t b = lo;
+	// FP32: two bits per sweep; FP64 keeps one (four double amplitudes per item cost the registers
+	// that hold two CTAs per SM)
+	for (; sizeof(T) == 4 && b + 1 < hi; b += 2) {
+		const uint32_t ba = 1u << b, bb = 2u << b;
+		const uint32_t items = (1u << k) >> 2;
+		for (uint32_t i = threadIdx.x; i < items; i += blockDim.x) {
+			// insert zeros at bits b and b + 1
+			const uint32_t i0 = ((i >> b) << (b + 2)) | (i & (ba - 1));
+			cplx_t<T> a00 = sm[i0], a10 = sm[i0 | ba], a01 = sm[i0 | bb], a11 = sm[i0 | ba | bb];
+			rx_pair<T>(a00, a10, m, L.form);
+			rx_pair<T>(a01, a11, m, L.form);
+			rx_pair<T>(a00, a01, m, L.form);
+			rx_pair<T>(a10, a11, m, L.form);
+			sm[i0] = a00;
+			sm[i0 | ba] = a10;
+			sm[i0 | bb] = a01;
+			sm[i0 | ba | bb] = a11;
+		}
+		__syncthreads();
+	}
+	for (; b < hi; ++b) {
 		const uint32_t bit = 1u << b;
+		const uint32_t items = (1u << k) >> 1;
 		for (uint32_t i = threadIdx.x; i < items; i += blockDim.x) {
 			const uint32_t i0 = ((i >> b) << (b + 1)) | (i & (bit - 1));
 			cplx_t<T> a0 = sm[i0], a1 = sm[i0 | bit];
-			if (L.form == 0) op2<T, Op1::UnitIm01, 0>(a0, a1, m);
-			else op2<T, Op1::UnitIm10, 0>(a0, a1, m);
+			rx_pair<T>(a0, a1, m, L.form);
 			sm[i0] = a0;
 			sm[i0 | bit] = a1;
 		}
