@@ -479,7 +479,8 @@ def run_qaoa(args):
             times.append(max_over_ranks(dist, time.perf_counter() - t0))
         amps = sum(1 << insts[i]["n"] for i in range(len(insts)))
         energies = replicas.gather_values(dist, mine, e, len(insts), device="cuda")
-        out[prec] = {"cluster": batch.cluster, "autotune_seconds": tuned, "seconds_per_launch": statistics.median(times),
+        out[prec] = {"cluster": batch.cluster, "tile": list(batch.tile), "autotune_seconds": tuned,
+                     "seconds_per_launch": statistics.median(times),
                      "instances_per_s": len(insts) / statistics.median(times),
                      "amplitude_layers_per_s": amps * 4 / statistics.median(times), "energies": energies}
         batch.close()

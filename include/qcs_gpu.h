@@ -166,6 +166,9 @@ int qcs_qaoa_batch_create(const qcs_qaoa_instance* instances, size_t count, uint
 int qcs_qaoa_batch_set_angles(qcs_qaoa_batch_handle b, const double* gammas, const double* betas);
 /* CTAs per thread-block cluster sharing one instance (1, 2, 4, 8 or 16; 0 before the first call: 8) */
 int qcs_qaoa_batch_set_cluster(qcs_qaoa_batch_handle b, int ctas);
+/* tile shape of the mixer passes over the high qubits: runs of 2^low contiguous amplitudes times
+ * `high` further qubits per pass (low >= 3, high >= 1, low + high <= 12; default 6 and 6) */
+int qcs_qaoa_batch_set_tile(qcs_qaoa_batch_handle b, int low, int high);
 /* runs every instance from |0..0>: H on all qubits, then p layers; energies_out (count doubles) gets
  * <H> = sum_x |psi_x|^2 E(x), E(x) = -(sum h_i s_i + sum J_ij s_i s_j) (IsingModel.h:106-119) */
 int qcs_qaoa_batch_run(qcs_qaoa_batch_handle b, double* energies_out);

@@ -100,6 +100,7 @@ SIGNATURES = {
     "qcs_qaoa_batch_create": (_i, [C.c_void_p, _sz, _u32, _i, C.POINTER(_h)]),
     "qcs_qaoa_batch_set_angles": (_i, [_h, _pd, _pd]),
     "qcs_qaoa_batch_set_cluster": (_i, [_h, _i]),
+    "qcs_qaoa_batch_set_tile": (_i, [_h, _i, _i]),
     "qcs_qaoa_batch_run": (_i, [_h, _pd]),
     "qcs_qaoa_batch_state": (_i, [_h, _sz, _pd]),
     "qcs_qaoa_batch_amplitudes": (_u64, [_h]),

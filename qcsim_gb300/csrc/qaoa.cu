@@ -81,6 +81,7 @@ template <typename T> struct QParams {
 	double* parts;                // energy partials
 	double* energies;             // out
 	double* scale2;               // |scale|^2 per instance
+	uint32_t stage_low, stage_high;  // mixer-pass tile: 2^stage_low contiguous amplitudes x stage_high qubits
 };
 
 // tile of the pass: qubits 0..L-1 and `nh` high qubits starting at `hq0`; the other qubits index tiles
@@ -234,7 +235,8 @@ __global__ void __launch_bounds__(kQThreads, 2) k_qaoa(QParams<T> P) {
 		cplx_t<T>* s = P.amps + I.offset;
 		const uint32_t n = I.n;
 		const uint32_t g0 = I.g0;
-		const uint32_t nstages = (n > g0) ? ((n - g0 + 5) / 6) : 0;  // high-qubit mixer passes
+		const uint32_t sh = P.stage_high;
+		const uint32_t nstages = (n > g0) ? ((n - g0 + sh - 1) / sh) : 0;  // high-qubit mixer passes
 		const int16_t* KL = P.kltab + I.kl;
 		TileGeo G0;  // the low-group geometry: tile = x_low, tile index = x_high
 		G0.n = n; G0.L = g0; G0.hq0 = g0; G0.nh = 0;
@@ -246,8 +248,8 @@ __global__ void __launch_bounds__(kQThreads, 2) k_qaoa(QParams<T> P) {
 			for (uint32_t stage = 0; stage <= nstages; ++stage) {
 				TileGeo G = G0;
 				if (stage > 0) {
-					const uint32_t lo = g0 + 6 * (stage - 1);
-					G.L = 6; G.hq0 = lo; G.nh = min(6u, n - lo);
+					const uint32_t lo = g0 + sh * (stage - 1);
+					G.L = P.stage_low; G.hq0 = lo; G.nh = min(sh, n - lo);
 				}
 				const uint64_t ntiles = G.ntiles();
 				const uint32_t K = G.size();
@@ -352,6 +354,7 @@ struct qcs_qaoa_batch {
 	cudaGraph_t graph = nullptr;
 	cudaGraphExec_t exec = nullptr;
 	int cluster = 0;               // CTAs per cluster (0: choose)
+	int stage_low = 6, stage_high = 6;  // mixer-pass tile shape
 	int sms = 148;
 	std::string err;
 };
@@ -385,6 +388,8 @@ cudaError_t launch(qcs_qaoa_batch* b) {
 	P.parts = b->d_parts;
 	P.energies = b->d_energies;
 	P.scale2 = b->d_scale2;
+	P.stage_low = static_cast<uint32_t>(b->stage_low);
+	P.stage_high = static_cast<uint32_t>(b->stage_high);
 	const size_t smem = (size_t(1) << qcs::kGroupBits) * sizeof(qcs::cplx_t<T>);
 	cudaError_t e = cudaFuncSetAttribute(qcs::k_qaoa<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
 	if (e == cudaSuccess) e = cudaFuncSetAttribute(qcs::k_qaoa<T>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
@@ -634,9 +639,9 @@ int qcs_qaoa_batch_set_angles(qcs_qaoa_batch_handle b, const double* gammas, con
 	return QCS_OK;
 }
 
-int qcs_qaoa_batch_set_cluster(qcs_qaoa_batch_handle b, int ctas) {
-	if (!b || ctas < 1 || ctas > 16 || (ctas & (ctas - 1))) return QCS_INVALID_ARGUMENT;
-	b->cluster = ctas;
+namespace {
+// the captured graph holds the launch configuration: drop it when the schedule changes
+void reset_graph(qcs_qaoa_batch* b) {
 	if (b->exec) {
 		cudaGraphExecDestroy(b->exec);
 		b->exec = nullptr;
@@ -645,6 +650,22 @@ int qcs_qaoa_batch_set_cluster(qcs_qaoa_batch_handle b, int ctas) {
 		cudaGraphDestroy(b->graph);
 		b->graph = nullptr;
 	}
+}
+}  // namespace
+
+int qcs_qaoa_batch_set_cluster(qcs_qaoa_batch_handle b, int ctas) {
+	if (!b || ctas < 1 || ctas > 16 || (ctas & (ctas - 1))) return QCS_INVALID_ARGUMENT;
+	b->cluster = ctas;
+	reset_graph(b);
+	return QCS_OK;
+}
+
+int qcs_qaoa_batch_set_tile(qcs_qaoa_batch_handle b, int low, int high) {
+	if (!b) return QCS_INVALID_ARGUMENT;
+	if (low < 3 || high < 1 || low + high > qcs::kGroupBits) return qfail(b, QCS_INVALID_ARGUMENT, "tile: low >= 3, high >= 1, low + high <= 12");
+	b->stage_low = low;
+	b->stage_high = high;
+	reset_graph(b);
 	return QCS_OK;
 }
 

@@ -15,6 +15,7 @@ import numpy as np
 from . import _lib as L
 
 CLUSTER_SIZES = (1, 2, 4, 8)  # CTAs per thread-block cluster (portable sizes)
+TILE_SHAPES = ((6, 6), (5, 7), (4, 8))  # mixer-pass tiles: (low contiguous qubits, high qubits per pass)
 
 
 class QaoaBatch:
@@ -37,6 +38,7 @@ class QaoaBatch:
         self._h = C.c_void_p()
         self.precision = precision
         self.cluster = 0
+        self.tile = (6, 6)
         prec = L.QCS_FP64 if precision == "fp64" else L.QCS_FP32
         L.check(self._lib.qcs_qaoa_batch_create(C.cast(arr, C.c_void_p), len(instances), p, prec, C.byref(self._h)))
         self.set_angles(np.array([inst["gammas"] for inst in instances]), np.array([inst["betas"] for inst in instances]))
@@ -54,6 +56,11 @@ class QaoaBatch:
         self._ck(self._lib.qcs_qaoa_batch_set_cluster(self._h, ctas))
         self.cluster = ctas
 
+    def set_tile(self, low: int, high: int) -> None:
+        """tile shape of the mixer passes: 2^low contiguous amplitudes times `high` further qubits"""
+        self._ck(self._lib.qcs_qaoa_batch_set_tile(self._h, low, high))
+        self.tile = (low, high)
+
     def shape_key(self, precision: str | None = None) -> str:
         """what the schedule depends on: precision, layer count and the instance-size histogram"""
         sizes: dict[int, int] = {}
@@ -62,31 +69,37 @@ class QaoaBatch:
         hist = ",".join(f"{n}:{c}" for n, c in sorted(sizes.items()))
         return f"{precision or self.precision}|p{self.p}|{hist}"
 
-    def autotune(self, candidates=CLUSTER_SIZES, reps: int = 2, cache: Path | None = None) -> dict:
-        """choose the cluster size (CTAs that share one instance's tiles) by timing one launch of each
-        candidate after a warm-up launch, keep the fastest, and return {size: seconds}.  With `cache`
-        (a JSON file), a choice recorded for the same shape key is reused without timing."""
+    def autotune(self, candidates=CLUSTER_SIZES, shapes=TILE_SHAPES, reps: int = 2, cache: Path | None = None) -> dict:
+        """choose the schedule (cluster size: CTAs sharing one instance's tiles) and the mixer-pass tile
+        shape by timing one launch of every combination after a warm-up launch; keep the fastest and
+        return {"cluster,low,high": seconds}.  With `cache` (a JSON file), a choice recorded for the
+        same shape key is reused without timing."""
         key = self.shape_key()
         table = {}
         if cache is not None and Path(cache).exists():
             table = json.loads(Path(cache).read_text())
             if key in table:
+                self.set_tile(*table[key]["tile"])
                 self.set_cluster(int(table[key]["cluster"]))
-                return {int(k): v for k, v in table[key]["seconds"].items()}
+                return dict(table[key]["seconds"])
         times = {}
-        for cl in candidates:
-            self.set_cluster(cl)
-            self.run()  # graph capture and warm-up
-            best = float("inf")
-            for _ in range(reps):
-                t0 = time.perf_counter()
-                self.run()
-                best = min(best, time.perf_counter() - t0)
-            times[cl] = best
+        for low, high in shapes:
+            self.set_tile(low, high)
+            for cl in candidates:
+                self.set_cluster(cl)
+                self.run()  # graph capture and warm-up
+                best = float("inf")
+                for _ in range(reps):
+                    t0 = time.perf_counter()
+                    self.run()
+                    best = min(best, time.perf_counter() - t0)
+                times[f"{cl},{low},{high}"] = best
         choice = min(times, key=times.get)
-        self.set_cluster(choice)
+        cl, low, high = (int(x) for x in choice.split(","))
+        self.set_tile(low, high)
+        self.set_cluster(cl)
         if cache is not None:
-            table[key] = {"cluster": choice, "seconds": times}
+            table[key] = {"cluster": cl, "tile": [low, high], "seconds": times}
             Path(cache).write_text(json.dumps(table, indent=1))
         return times
 
