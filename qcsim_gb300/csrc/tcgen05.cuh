@@ -108,5 +108,14 @@ __device__ __forceinline__ void bulk_wait_read() { asm volatile("cp.async.bulk.w
 // wait until this thread's committed bulk stores are complete
 __device__ __forceinline__ void bulk_wait_all() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
 
+// 16-byte asynchronous copy global -> shared, completed by cp_async_wait_all (per thread)
+__device__ __forceinline__ void cp_async16(void* dst, const void* src) {
+	asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_addr(dst)), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() {
+	asm volatile("cp.async.commit_group;" ::: "memory");
+	asm volatile("cp.async.wait_group 0;" ::: "memory");
+}
+
 }  // namespace tc
 }  // namespace qcs

@@ -370,20 +370,12 @@ __global__ void __launch_bounds__(THREADS) k_tile(cplx_t<T>* __restrict__ s, Til
 	__syncthreads();
 	for (uint64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
 		const uint64_t base = fixed_base(fixtab, tile);
-		// loads in batches of load_batch per thread, all issued before the first shared-memory store
-		for (uint32_t j0 = threadIdx.x; j0 < K; j0 += blockDim.x * load_batch<T>()) {
-			cplx_t<T> r[load_batch<T>()];
-#pragma unroll
-			for (int b = 0; b < load_batch<T>(); ++b) {
-				const uint32_t j = j0 + b * blockDim.x;
-				if (j < K) r[b] = s[base | highoff[j >> p.L] | (j & lowmask)];
-			}
-#pragma unroll
-			for (int b = 0; b < load_batch<T>(); ++b) {
-				const uint32_t j = j0 + b * blockDim.x;
-				if (j < K) sm[j] = r[b];
-			}
-		}
+		// asynchronous 16-byte copies (one FP64 or two FP32 amplitudes, inside one run of 2^L >= 32),
+		// all in flight at once without holding registers
+		constexpr uint32_t kPer = 16 / sizeof(cplx_t<T>);
+		for (uint32_t j = threadIdx.x * kPer; j < K; j += blockDim.x * kPer)
+			tc::cp_async16(sm + j, s + (base | highoff[j >> p.L] | (j & lowmask)));
+		tc::cp_async_wait_all();
 		__syncthreads();
 		for (uint32_t oi = 0; oi < p.op_count; ++oi) {
 			const TileOp op = opsrc[oi];
