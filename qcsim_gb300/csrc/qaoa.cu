@@ -33,6 +33,7 @@
 
 #include "engine.cuh"
 #include "gate_math.cuh"
+#include "tcgen05.cuh"
 
 namespace cg = cooperative_groups;
 
@@ -153,20 +154,11 @@ template <typename T> constexpr int qaoa_batch() { return sizeof(T) == 4 ? 4 : 2
 
 template <typename T>
 __device__ __forceinline__ void tile_load(cplx_t<T>* sm, const cplx_t<T>* s, const TileGeo& G, uint64_t t, uint32_t K) {
-	constexpr int B = qaoa_batch<T>();
-	for (uint32_t j0 = threadIdx.x; j0 < K; j0 += kQThreads * B) {
-		cplx_t<T> r[B];
-#pragma unroll
-		for (int b = 0; b < B; ++b) {
-			const uint32_t j = j0 + b * kQThreads;
-			if (j < K) r[b] = s[G.addr(t, j)];
-		}
-#pragma unroll
-		for (int b = 0; b < B; ++b) {
-			const uint32_t j = j0 + b * kQThreads;
-			if (j < K) sm[j] = r[b];
-		}
-	}
+	// asynchronous 16-byte copies (one FP64 or two FP32 amplitudes, inside one run of 2^L >= 2)
+	constexpr uint32_t kPer = 16 / sizeof(cplx_t<T>);
+	for (uint32_t j = threadIdx.x * kPer; j < K; j += kQThreads * kPer) tc::cp_async16(sm + j, s + G.addr(t, j));
+	tc::cp_async_wait_all();
+	__syncthreads();
 }
 
 template <typename T>
