@@ -342,11 +342,12 @@ def run_gb300(args):
                         "hbm_frac_per_gate": qb / (qft_ms / 1e3) / (peak * 1e9)}
 
     # the metric's second half on the same circuit: its first four layers on a fresh FP64 register and on
-    # a fused FP32 register (greedy blocks of at most 3 qubits), device time and fidelity
+    # fused FP32 registers (greedy blocks of at most 3 qubits; the learned partition), device time and fidelity
     if rank == 0 and not args.no_fused:
         fops = [op for lay in layers[:4] for op in lay]
-        extra["fused_fp32"] = {"workload": f"layers 0-3 of the circuit above ({len(fops)} gates)",
-                               **fused_vs_fp64(n, fops, 3, args.seed)}
+        extra["fused_fp32"] = {"workload": f"layers 0-3 of the circuit above ({len(fops)} gates); greedy blocks of at most "
+                                           "3 qubits, and the partition of the shipped learned cost model",
+                               **fused_vs_fp64(n, fops, 3, args.seed, learned=True)}
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -405,7 +406,7 @@ def read_traffic(kernel_family: str, n: int):
     return None
 
 
-def fused_vs_fp64(n: int, ops: list, max_block: int, seed: int = 1) -> dict:
+def fused_vs_fp64(n: int, ops: list, max_block: int, seed: int = 1, learned: bool = False) -> dict:
     """the same gate list on a plain FP64 register and on a fused FP32 register (greedy blocks of at most
     max_block qubits; 4- and 5-qubit blocks on the tensor cores): device time of each (the call includes
     the host-side planning) and the fidelity / max amplitude error of the FP32 result"""
@@ -417,11 +418,16 @@ def fused_vs_fp64(n: int, ops: list, max_block: int, seed: int = 1) -> dict:
     recs = G.records(ops)
     stream = torch.cuda.Stream()
     out, regs = {}, {}
-    for prec in ("fp64", "fp32"):
-        reg = Q.QubitRegister(n, seed=seed, precision=prec)
+    runs = ("fp64", "fp32", "learned") if learned else ("fp64", "fp32")
+    for prec in runs:
+        reg = Q.QubitRegister(n, seed=seed, precision="fp64" if prec == "fp64" else "fp32")
         lib.qcs_set_stream(reg.handle, stream.cuda_stream)
         if prec == "fp32":
             reg.set_fusion(1, max_block)
+        elif prec == "learned":
+            from qcsim_gb300 import costmodel
+            mlp, pass_ms = costmodel.load()  # the GPU-trained model shipped with the package
+            costmodel.attach(reg, mlp, pass_ms)
         reg.profile(True)
         torch.cuda.synchronize()
         a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -435,12 +441,18 @@ def fused_vs_fp64(n: int, ops: list, max_block: int, seed: int = 1) -> dict:
         regs[prec] = reg
     f, d = C.c_double(), C.c_double()
     L.check(lib.qcs_compare(regs["fp64"].handle, regs["fp32"].handle, C.byref(f), C.byref(d)), regs["fp64"].handle)
+    res = {"gates": len(ops), "max_block_qubits": max_block, "fp64_seconds": out["fp64"]["seconds"],
+           "fp32_fused_seconds": out["fp32"]["seconds"], "speedup": out["fp64"]["seconds"] / out["fp32"]["seconds"],
+           "one_minus_fidelity": 1.0 - f.value, "max_abs_amplitude_error": d.value,
+           "fp64_kernels": out["fp64"]["kernels"], "fp32_kernels": out["fp32"]["kernels"]}
+    if learned:
+        L.check(lib.qcs_compare(regs["fp64"].handle, regs["learned"].handle, C.byref(f), C.byref(d)), regs["fp64"].handle)
+        res["learned"] = {"seconds": out["learned"]["seconds"], "speedup": out["fp64"]["seconds"] / out["learned"]["seconds"],
+                          "one_minus_fidelity": 1.0 - f.value, "max_abs_amplitude_error": d.value,
+                          "kernels": out["learned"]["kernels"]}
     for r in regs.values():
         r.close()
-    return {"gates": len(ops), "max_block_qubits": max_block, "fp64_seconds": out["fp64"]["seconds"],
-            "fp32_fused_seconds": out["fp32"]["seconds"], "speedup": out["fp64"]["seconds"] / out["fp32"]["seconds"],
-            "one_minus_fidelity": 1.0 - f.value, "max_abs_amplitude_error": d.value,
-            "fp64_kernels": out["fp64"]["kernels"], "fp32_kernels": out["fp32"]["kernels"]}
+    return res
 
 
 def run_precision(args):
