@@ -566,7 +566,15 @@ int qcs_sample(qcs_handle h, const double* probs, size_t nshots, uint64_t* state
 int qcs_qubit_probability(qcs_handle h, uint32_t qubit, double* p_out) {
 	if (!h || !p_out) return QCS_INVALID_ARGUMENT;
 	if (qubit >= 63) return fail(h, QCS_INVALID_ARGUMENT, "qubit out of range");
-	return masked_prob(h, 1ULL << qubit, 1ULL << qubit, p_out);
+	// the pending global factor stays pending: amplitudes = scale x stored values, so the probability
+	// is |scale|^2 times the stored values' sum (no sweep folding the factor into the amplitudes)
+	cudaError_t e = h->prec == QCS_FP64 ? qcs::reduce_masked_prob<double>(static_cast<double2*>(h->d_state), h->N, 1ULL << qubit,
+	                                                                      1ULL << qubit, h->sc, h->sms, h->stream, p_out)
+	                                    : qcs::reduce_masked_prob<float>(static_cast<float2*>(h->d_state), h->N, 1ULL << qubit,
+	                                                                     1ULL << qubit, h->sc, h->sms, h->stream, p_out);
+	QCS_CK(h, e, "probability reduction");
+	*p_out *= std::norm(h->scale);
+	return QCS_OK;
 }
 
 int qcs_probabilities(qcs_handle h, double* host_out) {
