@@ -1,7 +1,7 @@
 // Learned cost model: a 3-layer MLP (F inputs -> 64 -> 64 -> 1, ReLU, FP32) that predicts the log of a
 // fused block's device time from its features.  Forward, backward and the Adam update are hand-written
-// kernels; the fuser queries the model through a host callback that runs the inference kernel on a
-// batch of candidate blocks.
+// kernels; the partition choice (costmodel.cu) runs the inference kernel on every block of each
+// candidate partition in one batch.
 #include <cmath>
 #include <cstring>
 #include <string>

@@ -1,6 +1,6 @@
 // Inline-PTX wrappers for the Blackwell tensor-core path (sm_100a / sm_103a): tensor memory
 // allocation, tcgen05.mma with shared-memory operand descriptors, tcgen05.commit to an mbarrier,
-// tensor-memory loads, and the bulk (TMA) copies between global and shared memory.
+// tensor-memory loads, and cp.async tile copies.
 //
 // Operand layout used throughout: K-major, no swizzle.  A core matrix is 8 rows x 16 bytes (four
 // 32-bit elements of one row stored contiguously, rows 16 bytes apart, 128 contiguous bytes); core
@@ -74,9 +74,6 @@ __device__ __forceinline__ void mbar_init(uint64_t* mbar, uint32_t count) {
 	asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(mbar)), "r"(count));
 	asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
 }
-__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* mbar, uint32_t bytes) {
-	asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(mbar)), "r"(bytes) : "memory");
-}
 // bounded wait for the phase with the given parity to complete; false when the bound ran out
 __device__ __forceinline__ bool mbar_wait(uint64_t* mbar, uint32_t parity, uint32_t max_tries) {
 	const uint32_t a = smem_addr(mbar);
@@ -91,22 +88,6 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* mbar, uint32_t parity, uint3
 	}
 	return false;
 }
-
-// bulk copy global -> shared (TMA, non-tensor); completes `bytes` on the mbarrier's transaction count
-__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* mbar) {
-	asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(smem_addr(dst)),
-	             "l"(src), "r"(bytes), "r"(smem_addr(mbar))
-	             : "memory");
-}
-// bulk copy shared -> global in this thread's bulk group
-__device__ __forceinline__ void bulk_s2g(void* dst, const void* src, uint32_t bytes) {
-	asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;" ::"l"(dst), "r"(smem_addr(src)), "r"(bytes) : "memory");
-}
-__device__ __forceinline__ void bulk_commit() { asm volatile("cp.async.bulk.commit_group;" ::: "memory"); }
-// wait until this thread's committed bulk stores have finished reading shared memory
-__device__ __forceinline__ void bulk_wait_read() { asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory"); }
-// wait until this thread's committed bulk stores are complete
-__device__ __forceinline__ void bulk_wait_all() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
 
 // 16-byte asynchronous copy global -> shared, completed by cp_async_wait_all (per thread)
 __device__ __forceinline__ void cp_async16(void* dst, const void* src) {
