@@ -9,8 +9,16 @@ qubit probability after every step.  The state (16 GiB) is larger than L2, so no
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
 
+The line also carries: the roofline of the dominant kernel (algorithmic bytes of the gates its launches
+applied over their CUDA-event time; DRAM traffic per launch from the committed ncu summary), the same
+layers with one kernel per gate (`per_gate`), QFT-30 (`qft`), the first four layers on fused FP32
+registers against FP64 (`fused_fp32`: greedy blocks of at most 3 qubits and the learned partition),
+SM clocks sampled during the timed region, and the CPU oracle on a bounded sample (`cpu_baseline`).
+
 --impl reference times the CPU oracle (a restatement of QCSim's QubitRegister loops, OpenMP on all
-host threads) on the same workload, a bounded number of gates per step.
+host threads) on the same workload, a bounded number of gates per step.  Other workloads:
+--config precision (fused FP32 vs FP64 on one circuit), qaoa (512-instance batch, sharded over ranks
+under torchrun), learned (the MLP partition vs greedy vs unfused on an unseen circuit).
 """
 from __future__ import annotations
 
