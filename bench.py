@@ -203,6 +203,38 @@ def cpu_baseline(args, ops, rank):
                       + ("" if n == args.qubits else f", scaled by 2^{n - args.qubits} to {args.qubits} qubits")}
 
 
+def small_config_both(seed: int) -> dict:
+    """the 20-qubit layered circuit of depth 40 (the CPU-sized configuration) end to end on the GPU
+    (one ApplyGates call, state resident) and on the CPU oracle with every host thread"""
+    import torch
+    import qcsim_gb300 as Q
+    from qcsim_gb300 import circuits, gates as G
+    from oracle import bind
+    ops = circuits.layered_circuit(20, 40, seed=seed)
+    recs = G.records(ops)
+    reg = Q.QubitRegister(20, seed=seed)
+    reg.apply_records(recs)  # warm-up
+    reg.setToBasisState(0)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    reg.apply_records(recs)
+    torch.cuda.synchronize()
+    gpu_s = time.perf_counter() - t0
+    gpu_state = reg.getRegisterStorage()
+    reg.close()
+    bind.build_oracle()
+    lib = bind.oracle()
+    lib.qo_set_threads(os.cpu_count() or 1)
+    ref = bind.OracleRegister(20)
+    t0 = time.perf_counter()
+    ref.apply(ops)
+    cpu_s = time.perf_counter() - t0
+    err = float(np.abs(gpu_state - ref.state()).max())
+    return {"workload": f"layered random circuit, 20 qubits, depth 40, seed {seed} ({len(ops)} gates)",
+            "gpu_seconds": gpu_s, "cpu_seconds": cpu_s, "cpu_cores": lib.qo_max_threads(), "gpu_gates_per_s": len(ops) / gpu_s,
+            "cpu_gates_per_s": len(ops) / cpu_s, "max_abs_amplitude_difference": err}
+
+
 def run_reference(args):
     rank, world, local, dist = dist_init(args)
     if rank != 0:
@@ -360,6 +392,7 @@ def run_gb300(args):
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         cpu = cpu_baseline(args, ops, rank)
+        extra["c0"] = small_config_both(args.seed)
 
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": "gates/s", "n_gpus": world, "steps": args.steps,

@@ -12,12 +12,16 @@ namespace {
 constexpr int kThreads = 256;
 
 template <typename A, typename B>
-__global__ void __launch_bounds__(kThreads) k_compare(const A* __restrict__ a, const B* __restrict__ b, uint64_t N, double* part) {
+__global__ void __launch_bounds__(kThreads) k_compare(const A* __restrict__ a, const B* __restrict__ b, uint64_t N, double2 sa,
+                                                      double2 sb, double* part) {
 	__shared__ double sh[5][kThreads];
 	const uint64_t stride = static_cast<uint64_t>(gridDim.x) * blockDim.x;
 	double re = 0, im = 0, na = 0, nb = 0, mx = 0;
 	for (uint64_t i = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < N; i += stride) {
-		const double ax = a[i].x, ay = a[i].y, bx = b[i].x, by = b[i].y;
+		// amplitude = pending factor x stored value, in double
+		const double sx = a[i].x, sy = a[i].y, tx = b[i].x, ty = b[i].y;
+		const double ax = sa.x * sx - sa.y * sy, ay = sa.x * sy + sa.y * sx;
+		const double bx = sb.x * tx - sb.y * ty, by = sb.x * ty + sb.y * tx;
 		re += ax * bx + ay * by;
 		im += ax * by - ay * bx;
 		na += ax * ax + ay * ay;
@@ -43,12 +47,12 @@ __global__ void __launch_bounds__(kThreads) k_compare(const A* __restrict__ a, c
 }
 
 template <typename A, typename B>
-cudaError_t run(const void* a, const void* b, uint64_t N, int sms, cudaStream_t st, double out[5]) {
+cudaError_t run(const void* a, const void* b, uint64_t N, double2 sa, double2 sb, int sms, cudaStream_t st, double out[5]) {
 	const int g = grid_for(N, kThreads, sms, 4);
 	double* d = nullptr;
 	cudaError_t e = cudaMalloc(&d, sizeof(double) * 5 * g);
 	if (e != cudaSuccess) return e;
-	k_compare<A, B><<<g, kThreads, 0, st>>>(static_cast<const A*>(a), static_cast<const B*>(b), N, d);
+	k_compare<A, B><<<g, kThreads, 0, st>>>(static_cast<const A*>(a), static_cast<const B*>(b), N, sa, sb, d);
 	note_launches(1);
 	std::vector<double> h(5 * static_cast<size_t>(g));
 	e = cudaGetLastError();
@@ -73,18 +77,18 @@ extern "C" int qcs_compare(qcs_handle h, qcs_handle other, double* fidelity_out,
 		h->err = "registers differ in size";
 		return QCS_INVALID_ARGUMENT;
 	}
-	// pending global factors are folded in first (both registers)
-	double dummy = 0;
-	if (int st = qcs_qubit_probability(h, 0, &dummy)) return st;
-	if (int st = qcs_qubit_probability(other, 0, &dummy)) return st;
+	// each register's pending global factor is applied inside the sweep (the stored values stay as they are);
+	// the other register's queued work finishes first, the comparison runs on this register's stream
 	cudaError_t e = cudaStreamSynchronize(other->stream);
 	double r[5] = {0, 0, 0, 0, 0};
+	const double2 sa = make_double2(h->scale.real(), h->scale.imag());
+	const double2 sb = make_double2(other->scale.real(), other->scale.imag());
 	if (e == cudaSuccess) {
 		const bool a64 = h->prec == QCS_FP64, b64 = other->prec == QCS_FP64;
-		if (a64 && b64) e = qcs::run<double2, double2>(h->d_state, other->d_state, h->N, h->sms, h->stream, r);
-		else if (a64) e = qcs::run<double2, float2>(h->d_state, other->d_state, h->N, h->sms, h->stream, r);
-		else if (b64) e = qcs::run<float2, double2>(h->d_state, other->d_state, h->N, h->sms, h->stream, r);
-		else e = qcs::run<float2, float2>(h->d_state, other->d_state, h->N, h->sms, h->stream, r);
+		if (a64 && b64) e = qcs::run<double2, double2>(h->d_state, other->d_state, h->N, sa, sb, h->sms, h->stream, r);
+		else if (a64) e = qcs::run<double2, float2>(h->d_state, other->d_state, h->N, sa, sb, h->sms, h->stream, r);
+		else if (b64) e = qcs::run<float2, double2>(h->d_state, other->d_state, h->N, sa, sb, h->sms, h->stream, r);
+		else e = qcs::run<float2, float2>(h->d_state, other->d_state, h->N, sa, sb, h->sms, h->stream, r);
 	}
 	if (e != cudaSuccess) {
 		h->err = std::string("compare: ") + cudaGetErrorString(e);

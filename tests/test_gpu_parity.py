@@ -481,3 +481,31 @@ def test_larger_register_properties(Q):
     inv =[(type(g)(*(-x for x in g.params()[:1])) if hasattr(g, "theta") else g, *q) for (g, *q) in reversed(ops)]
     reg.ApplyGates(inv)
     assert abs(reg.getBasisStateAmplitude(0) - 1) < 1e-11
+
+
+@pytest.mark.parametrize("other_precision", ["fp64", "fp32"])
+def test_compare_applies_pending_factors(Q, other_precision):
+    """qcs_compare against amplitudes read back on the host: one register carries a pending global
+    factor (Hadamards and rotations applied one at a time, whose real factors stay on the host), the other
+    runs the same gates as one list; fidelity and max amplitude difference match the host figures"""
+    import ctypes as C
+    from qcsim_gb300 import _lib as L, gates as G
+    n = 14
+    ops = [(G.HadamardGate(), q) for q in range(n)] + [(G.RxGate(0.3 + 0.1 * q), q) for q in range(n)]
+    ops += [(G.CNOTGate(), q, (q + 5) % n) for q in range(n)] + [(G.RyGate(-0.7), q) for q in range(0, n, 3)]
+    a = Q.QubitRegister(n, seed=1)
+    a.set_passes(False)
+    for g, *qs in ops:
+        a.ApplyGate(g, *qs)
+    b = Q.QubitRegister(n, seed=1, precision=other_precision)
+    b.ApplyGates(ops)
+    lib = L.load()
+    f, d = C.c_double(), C.c_double()
+    L.check(lib.qcs_compare(a.handle, b.handle, C.byref(f), C.byref(d)), a.handle)
+    va, vb = a.getRegisterStorage(), b.getRegisterStorage().astype(np.complex128)
+    tol = 1e-13 if other_precision == "fp64" else 1e-6
+    assert abs(d.value - np.abs(va - vb).max()) < tol
+    assert abs(f.value - abs(np.vdot(va, vb)) ** 2 / (np.vdot(va, va).real * np.vdot(vb, vb).real)) < 1e-12
+    assert d.value < (1e-12 if other_precision == "fp64" else 1e-5)
+    a.close()
+    b.close()
