@@ -11,9 +11,12 @@ qubit probability after every step.  The state (16 GiB) is larger than L2, so no
 
 The line also carries: the roofline of the dominant kernel (algorithmic bytes of the gates its launches
 applied over their CUDA-event time; DRAM traffic per launch from the committed ncu summary), the same
-layers with one kernel per gate (`per_gate`), QFT-30 (`qft`), the first four layers on fused FP32
-registers against FP64 (`fused_fp32`: greedy blocks of at most 3 qubits and the learned partition),
-SM clocks sampled during the timed region, and the CPU oracle on a bounded sample (`cpu_baseline`).
+kernel's FP64-compute ceiling (`fp64_roofline`: FP64 instructions of its gate arithmetic per second
+against cuBLAS DGEMM measured in the same run), the same layers with one kernel per gate (`per_gate`),
+QFT-30 (`qft`), the first four layers on fused FP32 registers against FP64 (`fused_fp32`: greedy blocks
+of at most 3 qubits and the learned partition), the 20-qubit depth-40 circuit timed whole on the GPU and
+on the CPU oracle (`c0`), SM clocks sampled during the timed region, and the CPU oracle on a bounded
+sample (`cpu_baseline`).
 
 --impl reference times the CPU oracle (a restatement of QCSim's QubitRegister loops, OpenMP on all
 host threads) on the same workload, a bounded number of gates per step.  Other workloads:
@@ -318,7 +321,8 @@ def run_gb300(args):
         torch.cuda.synchronize()
         barrier(dist)
     launches = lib.qcs_launch_count() - launches0
-    prof = reg.read_profile()
+    prof_ops = reg.read_profile(fp_ops=True)
+    prof = {k: v[:3] for k, v in prof_ops.items()}
     reg.profile(False)
     ms = e0.elapsed_time(e1)
     ms_max = max_over_ranks(dist, ms)
@@ -326,6 +330,7 @@ def run_gb300(args):
     peak, peak_kind = peaks()
     hbm_frac = alg_bytes / (ms / 1e3) / (peak * 1e9)
     roofline = roofline_of(prof, peak, peak_kind, n, alg_bytes)
+    fp64_roof = fp64_roofline_of(prof_ops, roofline["kernel"], dgemm_tflops())
 
     # end to end through the C ABI: host gate records in, a qubit probability out, every step
     barrier(dist)
@@ -402,7 +407,7 @@ def run_gb300(args):
                                        f"{args.depth}, Toffoli/CCZ at 5% of positions, seed {args.seed}; one layer "
                                        "per step", "qubits": n, "gates_timed": gates, "parallelism": f"replicas{world}",
                            "l2": "state (16 GiB) larger than L2"},
-                "hbm_frac_per_gate": hbm_frac, "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
+                "hbm_frac_per_gate": hbm_frac, "roofline": roofline, "fp64_roofline": fp64_roof, "cpu_baseline": cpu, "e2e": e2e,
                 "clocks": clk.summary(), "gpu_launches": int(launches), **extra}
         print(json.dumps(line))
     if dist is not None:
@@ -430,6 +435,38 @@ def roofline_of(prof: dict, peak: float, peak_kind: str, n: int, gate_bytes: flo
             "algorithmic_bytes_per_launch": alg_per_launch, "avg_launch_ms": ms / launches,
             "pass_bytes_per_launch": pass_bytes / launches, "pass_GBps": pass_bytes / launches / avg_s / 1e9,
             "share_of_device_time": ms / total, "launches": launches}
+
+
+def dgemm_tflops(size: int = 4096) -> float:
+    """the GPU's FP64 rate: cuBLAS DGEMM (torch.matmul on float64, size^3, best of 3 after a warm-up
+    call), in TFLOP/s"""
+    import torch
+    a = torch.randn(size, size, dtype=torch.float64, device="cuda")
+    b = torch.randn_like(a)
+    c = torch.matmul(a, b)
+    best = float("inf")
+    for _ in range(3):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        torch.matmul(a, b, out=c)
+        e1.record()
+        e1.synchronize()
+        best = min(best, e0.elapsed_time(e1))
+    del a, b, c
+    return 2.0 * size ** 3 / (best / 1e3) / 1e12
+
+
+def fp64_roofline_of(prof_ops: dict, kernel: str, dgemm: float) -> dict:
+    """the FP64-compute ceiling of a kernel family: floating-point instructions its launches issued (the
+    engine counts them per pass from the gate forms: an FMA, multiply or add on an amplitude component is
+    one) per second of its device time, against the DGEMM rate in instructions (one FMA = one
+    instruction = two flops)"""
+    launches, ms, _, ops = prof_ops[kernel]
+    achieved = ops / (ms / 1e3) / 1e12
+    peak = dgemm / 2.0
+    return {"bound": "fp64", "kernel": kernel, "achieved": achieved, "peak": peak, "unit": "T FP64 instr/s",
+            "frac": achieved / peak, "fp_ops_per_launch": ops / launches,
+            "peak_source": "cuBLAS DGEMM 4096^3 measured in this run, one instruction per FMA", "dgemm_tflops": dgemm}
 
 
 def read_traffic(kernel_family: str, n: int):

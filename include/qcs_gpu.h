@@ -229,13 +229,16 @@ int qcs_set_option(qcs_handle h, int option, int value);
 /* ---- launch timing (no reference counterpart: the reference has no profiler) ----
  * When enabled, every kernel the register launches is bracketed by CUDA events on its stream.
  * qcs_profile_read synchronises the stream, returns per kernel family the launch count, the summed
- * device milliseconds and the summed algorithmic bytes (2 x amplitude bytes x amplitudes the launch
- * must read and write), and clears the records. */
+ * device milliseconds, the summed algorithmic bytes (2 x amplitude bytes x amplitudes the launch
+ * must read and write) and the summed floating-point instructions of the launches' gate arithmetic
+ * (FMA, multiply or add on an amplitude component: one each, in the register's precision; counted for
+ * the shared-memory passes on the CUDA cores, 0 for the other families), and clears the records. */
 typedef struct qcs_profile_entry {
 	char name[48];
 	uint64_t launches;
 	double milliseconds;
 	double bytes;
+	double fp_ops;
 } qcs_profile_entry;
 int qcs_profile_enable(qcs_handle h, int enable);
 int qcs_profile_read(qcs_handle h, qcs_profile_entry* out, int capacity, int* count_out);

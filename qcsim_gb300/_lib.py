@@ -138,7 +138,8 @@ class qcs_qaoa_instance(C.Structure):
 
 
 class qcs_profile_entry(C.Structure):
-    _fields_ = [("name", C.c_char * 48), ("launches", C.c_uint64), ("milliseconds", C.c_double), ("bytes", C.c_double)]
+    _fields_ = [("name", C.c_char * 48), ("launches", C.c_uint64), ("milliseconds", C.c_double), ("bytes", C.c_double),
+                ("fp_ops", C.c_double)]
 
 
 _lib = None

@@ -173,6 +173,44 @@ bool op_in_bounds(const TileOp& op, int k, size_t mats) {
 	return op.mat + need <= mats;
 }
 
+// floating-point instructions (FMA, multiply or add: one each) that one work item of a pass operation
+// issues, read off the forms in gate_math.cuh and tile_kernels.cu; tensor-core blocks count 0 here
+// (their products run on the tensor pipe)
+double fp_ops_per_item(const TileOp& op) {
+	const TKind kind = static_cast<TKind>(op.kind);
+	if (kind == TKind::Ctrl1q || kind == TKind::GlobalDiag) {
+		switch (static_cast<Op1>(op.op)) {
+		case Op1::Diag: return kind == TKind::GlobalDiag ? 4 : 8;  // one or two complex products
+		case Op1::Phase: return 4;
+		case Op1::PhaseI: return 2;
+		case Op1::Antidiag: case Op1::Real: case Op1::RxLike: return 8;
+		case Op1::Generic: return 16;
+		case Op1::UnitRe01: case Op1::UnitRe10: case Op1::UnitIm01: case Op1::UnitIm10: return 4;
+		default: return 0;  // sign flips, unit factors and moves
+		}
+	}
+	switch (kind) {
+	case TKind::PhaseRow: return 8;  // the root from its two table factors, then the amplitude product
+	case TKind::Dense2: return 4 * 16;
+	case TKind::Dense3: return 4 * 64;
+	case TKind::DenseN: return 4.0 * static_cast<double>(1u << (2 * op.nins));
+	default: return 0;
+	}
+}
+
+// a pass's floating-point instructions: per operation, work items per tile x tiles it runs in
+// (non-tile controls halve the tiles each; a non-tile phase target runs in half of them)
+double pass_fp_ops(const TilePass& tp, const std::vector<TileOp>& ops, int n) {
+	double total = 0;
+	for (uint32_t i = tp.op_begin; i < tp.op_begin + tp.op_count; ++i) {
+		const TileOp& op = ops[i];
+		double tiles = std::ldexp(1.0, n - tp.k - popcount64(op.gmask));
+		if (static_cast<TKind>(op.kind) == TKind::GlobalDiag && static_cast<Op1>(op.op) != Op1::Diag) tiles *= 0.5;
+		total += tiles * static_cast<double>((1u << tp.k) >> op.nins) * fp_ops_per_item(op);
+	}
+	return total;
+}
+
 template <typename T>
 int run_planned(qcs_handle h, const std::vector<PlannedPass>& passes, int kmax, int L0) {
 	const int n = static_cast<int>(h->n);
@@ -352,7 +390,8 @@ int run_planned(qcs_handle h, const std::vector<PlannedPass>& passes, int kmax, 
 	auto* s = static_cast<cplx_t<T>*>(h->d_state);
 	for (size_t i = 0; i < tps.size() && e == cudaSuccess; ++i) {
 		if (tps[i].op_count > 0) {
-			prof_begin(h, tps[i].dense == 2 ? "tile_pass_tc" : "tile_pass", 2.0 * sizeof(cplx_t<T>) * static_cast<double>(h->N));
+			prof_begin(h, tps[i].dense == 2 ? "tile_pass_tc" : "tile_pass", 2.0 * sizeof(cplx_t<T>) * static_cast<double>(h->N),
+			           h->prof ? pass_fp_ops(tps[i], ops, static_cast<int>(h->n)) : 0.0);
 			e = launch_tile_pass<T>(s, tps[i], static_cast<const TileOp*>(bb->d_ops), static_cast<const cplx_t<T>*>(bb->d_mats), h->sms,
 			                        h->stream, bb->d_err);
 			prof_end(h);

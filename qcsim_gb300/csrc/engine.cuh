@@ -106,8 +106,9 @@ struct qcs_register {
 
 namespace qcs {
 
-// launch timing (profile.cu): no-ops unless profiling is enabled on the register
-void prof_begin(qcs_handle h, const char* name, double bytes);
+// launch timing (profile.cu): no-ops unless profiling is enabled on the register; fp_ops = the
+// floating-point instructions the launch's gate arithmetic issues, where the launcher counts them
+void prof_begin(qcs_handle h, const char* name, double bytes, double fp_ops = 0);
 void prof_end(qcs_handle h);
 void prof_release(qcs_handle h);
 

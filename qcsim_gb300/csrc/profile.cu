@@ -14,7 +14,7 @@ namespace {
 
 struct Rec {
 	std::string name;
-	double bytes;
+	double bytes, fp_ops;
 	cudaEvent_t a, b;
 };
 
@@ -37,10 +37,10 @@ cudaEvent_t take(Prof* p) {
 
 }  // namespace
 
-void prof_begin(qcs_handle h, const char* name, double bytes) {
+void prof_begin(qcs_handle h, const char* name, double bytes, double fp_ops) {
 	Prof* p = static_cast<Prof*>(h->prof);
 	if (!p) return;
-	Rec r{name, bytes, take(p), take(p)};
+	Rec r{name, bytes, fp_ops, take(p), take(p)};
 	cudaEventRecord(r.a, h->stream);
 	p->recs.push_back(r);
 	p->open = true;
@@ -88,7 +88,7 @@ int qcs_profile_read(qcs_handle h, qcs_profile_entry* out, int capacity, int* co
 	}
 	struct Agg {
 		uint64_t n = 0;
-		double ms = 0, bytes = 0;
+		double ms = 0, bytes = 0, fp_ops = 0;
 	};
 	std::map<std::string, Agg> agg;
 	for (qcs::Rec& r : p->recs) {
@@ -98,6 +98,7 @@ int qcs_profile_read(qcs_handle h, qcs_profile_entry* out, int capacity, int* co
 		a.n += 1;
 		a.ms += ms;
 		a.bytes += r.bytes;
+		a.fp_ops += r.fp_ops;
 		p->pool.push_back(r.a);
 		p->pool.push_back(r.b);
 	}
@@ -110,6 +111,7 @@ int qcs_profile_read(qcs_handle h, qcs_profile_entry* out, int capacity, int* co
 			out[i].launches = kv.second.n;
 			out[i].milliseconds = kv.second.ms;
 			out[i].bytes = kv.second.bytes;
+			out[i].fp_ops = kv.second.fp_ops;
 		}
 		++i;
 	}

@@ -100,14 +100,19 @@ class QubitRegister:
         """bracket every kernel launch of this register with CUDA events (see read_profile)"""
         self._ck(self._lib.qcs_profile_enable(self._h, int(bool(enable))))
 
-    def read_profile(self) -> dict:
-        """{kernel family: (launches, device ms, algorithmic bytes)} since the last read"""
+    def read_profile(self, fp_ops: bool = False) -> dict:
+        """{kernel family: (launches, device ms, algorithmic bytes[, floating-point instructions])} since
+        the last read"""
         cap = 64
         arr = (L.qcs_profile_entry * cap)()
         n = C.c_int()
         self._ck(self._lib.qcs_profile_read(self._h, C.cast(arr, C.c_void_p), cap, C.byref(n)))
-        return {arr[i].name.decode(): (int(arr[i].launches), float(arr[i].milliseconds), float(arr[i].bytes))
-                for i in range(n.value)}
+        out = {}
+        for i in range(n.value):
+            e = arr[i]
+            row = (int(e.launches), float(e.milliseconds), float(e.bytes))
+            out[e.name.decode()] = row + (float(e.fp_ops),) if fp_ops else row
+        return out
 
     def seed(self, s: int) -> None:
         """reseed the register's generator (the reference's protected rng, QubitRegister.h:723)"""

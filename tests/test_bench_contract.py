@@ -47,3 +47,12 @@ def test_roofline_helpers():
     prof = {"tile_pass": (2, 10.0, 4.0e9), "ctrl1q_swap": (1, 1.0, 1.0e9)}
     r = bench.roofline_of(prof, 6791.0, "measured", 30, 123.0)
     assert r["algorithmic_bytes_per_launch"] == pytest.approx(2.0e9)
+
+
+def test_fp64_roofline_helper():
+    import bench
+    prof = {"tile_pass": (4, 100.0, 4 * 34359738368.0, 4 * 2.0e10)}
+    r = bench.fp64_roofline_of(prof, "tile_pass", 1.2)
+    assert r["bound"] == "fp64" and r["fp_ops_per_launch"] == pytest.approx(2.0e10)
+    assert r["achieved"] == pytest.approx(8.0e10 / 0.1 / 1e12)
+    assert r["peak"] == pytest.approx(0.6) and r["frac"] == pytest.approx(r["achieved"] / 0.6)

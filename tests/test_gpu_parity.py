@@ -509,3 +509,22 @@ def test_compare_applies_pending_factors(Q, other_precision):
     assert d.value < (1e-12 if other_precision == "fp64" else 1e-5)
     a.close()
     b.close()
+
+
+def test_pass_fp_op_count(Q):
+    """the profile's floating-point instruction count of a shared-memory pass follows the gate forms: a
+    factored rotation is one FMA per real component of each amplitude (2 per amplitude), a phase one
+    complex product on half the amplitudes (2 per amplitude), a CNOT none"""
+    from qcsim_gb300 import gates as G
+    n = 16
+    N = 1 << n
+    reg = Q.QubitRegister(n, seed=1)
+    reg.ApplyGates([(G.HadamardGate(), q) for q in range(n)])  # planning warm-up
+    reg.profile(True)
+    reg.read_profile()
+    reg.ApplyGates([(G.RxGate(0.3), 3), (G.RzGate(0.2), 5), (G.CNOTGate(), 1, 7), (G.RyGate(0.4), 14)])
+    prof = reg.read_profile(fp_ops=True)
+    assert set(prof) == {"tile_pass"}, prof
+    launches, _, _, ops = prof["tile_pass"]
+    assert launches == 1 and ops == 6 * N, (launches, ops)
+    reg.close()
