@@ -108,6 +108,12 @@ int qcs_apply_gate(qcs_handle h, const double* m, uint32_t k, uint32_t q0, uint3
 int qcs_apply_gates(qcs_handle h, const qcs_gate* gates, size_t count);
 /* ApplyOperatorMatrix (QubitRegister.h:499-505): dense 2^n x 2^n operator, row-major interleaved */
 int qcs_apply_operator_matrix(qcs_handle h, const double* m);
+/* The work of SubAlgo::NQubitsQuantumGate (NQubitsQuantumGate.h:20-46) and
+ * SubAlgo::NQubitsControlledQuantumGate (NQubitsControlledQuantumGate.h:20-60) without their 2^n x 2^n
+ * extended matrix: a dense 2^k x 2^k operator m (row-major, interleaved; 1 <= k <= 10) on the target
+ * qubits qubits[0..k-1] (matrix bit j = qubits[j]), applied to the amplitudes whose control qubits
+ * (the set bits of ctrl_mask) are all one; the others are unchanged. */
+int qcs_apply_operator_on_qubits(qcs_handle h, const double* m, uint32_t k, const uint32_t* qubits, uint64_t ctrl_mask);
 /* QuantumFourierTransform::QFT / IQFT on qubits [start, end] (QuantumFourierTransform.h:35-87) with
  * the mirror swaps of QubitsSwapper::Swap (QubitsSwapper.h:23-34) when do_swap != 0 */
 int qcs_qft(qcs_handle h, uint32_t start, uint32_t end, int inverse, int do_swap);

@@ -66,6 +66,7 @@ _REF_SIG = {
     "qr_qaoa_exec": (_i, [_h, _u32, _u32, _pu32, _pd, _pd, _u32, _pd, _pd]),
     "qr_ising_energy": (_d, [_u32, _u32, _pu32, _pd, _pd, _u64]),
     "qr_uniforms": (None, [_u64, _sz, _pd]),
+    "qr_nqubits_gate": (_i, [_h, _u32, _pd, _u32, _u32, _i, _pd]),
 }
 
 _oracle = None

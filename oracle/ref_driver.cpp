@@ -16,6 +16,8 @@
 #include "QuantumGate.h"
 #include "QuantumFourierTransform.h"
 #include "IsingModel.h"
+#include "NQubitsQuantumGate.h"
+#include "NQubitsControlledQuantumGate.h"
 
 #include "qcs_oracle.h"  // gate codes and the qo_gate record layout
 
@@ -246,6 +248,34 @@ double qr_ising_energy(uint32_t n, uint32_t nedges, const uint32_t* edges, const
 	std::vector<double> hv(h, h + n);
 	q.Set(ints, hv);
 	return q.Energy(state);
+}
+
+// SubAlgo::NQubitsQuantumGate (ctrl < 0) or NQubitsControlledQuantumGate (controlling qubit ctrl) of the
+// 2^k x 2^k operator op (row-major interleaved) at startQubit on an n-qubit register: its extended
+// matrix (getOperatorMatrix, row-major interleaved into ext_out) and, when r is given, Execute on r
+// (QubitRegister::ApplyOperatorMatrix of that matrix)
+int qr_nqubits_gate(void* r, uint32_t n, const double* op, uint32_t k, uint32_t start, int ctrl, double* ext_out) {
+	const Eigen::Index D = Eigen::Index(1) << k, NB = Eigen::Index(1) << n;
+	Mat U(D, D);
+	for (Eigen::Index i = 0; i < D; ++i)
+		for (Eigen::Index j = 0; j < D; ++j) U(i, j) = std::complex<double>(op[2 * (i * D + j)], op[2 * (i * D + j) + 1]);
+	Mat ext;
+	if (ctrl < 0) {
+		QC::SubAlgo::NQubitsQuantumGate<> g(n, U, start);
+		ext = g.getOperatorMatrix();
+		if (r) g.Execute(*static_cast<SeededRegister*>(r));
+	} else {
+		QC::SubAlgo::NQubitsControlledQuantumGate<> g(n, U, start, static_cast<size_t>(ctrl));
+		ext = g.getOperatorMatrix();
+		if (r) g.Execute(*static_cast<SeededRegister*>(r));
+	}
+	if (ext_out)
+		for (Eigen::Index i = 0; i < NB; ++i)
+			for (Eigen::Index j = 0; j < NB; ++j) {
+				ext_out[2 * (i * NB + j)] = ext(i, j).real();
+				ext_out[2 * (i * NB + j) + 1] = ext(i, j).imag();
+			}
+	return 0;
 }
 
 // one draw of std::uniform_real_distribution<double>(0,1) on std::mt19937_64(seed), as the register uses it

@@ -1,9 +1,12 @@
 """Sub-algorithms of the hot path, mirroring QCSim's QC::SubAlgo classes over the engine:
-QuantumFourierTransform (QuantumFourierTransform.h:12-92), QubitsSwapper (QubitsSwapper.h:10-43) and
-OneQubitGateTransform / HadamardTransform / XTransform (HadamardTransform.h:9-41).
+QuantumFourierTransform (QuantumFourierTransform.h:12-92), QubitsSwapper (QubitsSwapper.h:10-43),
+OneQubitGateTransform / HadamardTransform / XTransform (HadamardTransform.h:9-41), and the dense
+operator gates NQubitsQuantumGate (NQubitsQuantumGate.h:9-78) / NQubitsControlledQuantumGate
+(NQubitsControlledQuantumGate.h:9-97).
 
 The QFT runs as one engine call (qcs_qft), which applies the reference's gate sequence; the one-qubit
-transforms run as one gate list (qcs_one_qubit_transform).
+transforms run as one gate list (qcs_one_qubit_transform); the dense operator gates run as one
+qcs_apply_operator_on_qubits call on their 2^k x 2^k operator.
 """
 from __future__ import annotations
 
@@ -108,3 +111,74 @@ class HadamardTransform(OneQubitGateTransform):
 
 class XTransform(OneQubitGateTransform):
     gate_class = G.PauliXGate
+
+
+def _operator_qubits(op) -> int:
+    """getOperatorQubitsNumber (NQubitsQuantumGate.h:61-72): the bit length of rows - 1"""
+    return int(op.shape[0] - 1).bit_length()
+
+
+class NQubitsQuantumGate(QuantumSubAlgorithmOnSubregister):
+    """SubAlgo::NQubitsQuantumGate: a dense 2^k x 2^k operator on qubits startQubit .. startQubit + k - 1.
+
+    The reference's Execute (NQubitsQuantumGate.h:20-25) builds the 2^N x 2^N extended matrix and applies
+    it with ApplyOperatorMatrix; here the operator itself goes to the device (ApplyOperatorOnQubits), and
+    the extended matrix is built only for a register that records its gates (the log then holds what the
+    reference's log holds).  The reference's end qubit is startQubit + k clamped to N - 1
+    (QuantumAlgorithm.h:228-231), so its extended matrix stays within the operator's bounds only when the
+    operator reaches the top qubit (startQubit + k = N, the placement PhaseEstimation uses); there the two
+    agree exactly, and elsewhere this class applies the operator on its k qubits."""
+
+    def __init__(self, N: int, op, startQubit: int = 0):
+        self.U = np.array(op, dtype=np.complex128)
+        k = _operator_qubits(self.U)
+        if self.U.shape != (1 << k, 1 << k) or startQubit + k > N:
+            raise ValueError("the operator must be 2^k x 2^k and fit on qubits startQubit .. N - 1")
+        super().__init__(N, startQubit, startQubit + k)
+        self.nrQubits = N
+
+    def targets(self) -> list[int]:
+        return list(range(self.getStartQubit(), self.getStartQubit() + self.getRawOperatorQubitsNumber()))
+
+    def controls(self) -> list[int]:
+        return []
+
+    def Execute(self, reg) -> int:
+        if reg.recordGates:
+            reg.ApplyOperatorMatrix(self.getOperatorMatrix())
+        else:
+            reg.ApplyOperatorOnQubits(self.U, self.targets(), self.controls())
+        return 0
+
+    def getOperatorMatrix(self) -> np.ndarray:
+        """the 2^N x 2^N extended matrix: identity on the other qubits (and, controlled, where the control
+        is zero)"""
+        s, k = self.getStartQubit(), self.getRawOperatorQubitsNumber()
+        ext = np.kron(np.eye(1 << (self.nrQubits - s - k)), np.kron(self.U, np.eye(1 << s)))
+        for c in self.controls():
+            on = ((np.arange(1 << self.nrQubits) >> c) & 1).astype(bool)
+            ext = np.where(np.outer(on, on), ext, np.eye(1 << self.nrQubits))
+        return ext
+
+    def getRawOperatorMatrix(self) -> np.ndarray:
+        return self.U
+
+    def getRawOperatorQubitsNumber(self) -> int:
+        return _operator_qubits(self.U)
+
+
+class NQubitsControlledQuantumGate(NQubitsQuantumGate):
+    """SubAlgo::NQubitsControlledQuantumGate (NQubitsControlledQuantumGate.h:9-97): the operator where the
+    controlling qubit is one, the identity where it is zero"""
+
+    def __init__(self, N: int, op, startQubit: int = 1, controllingQubit: int = 0):
+        super().__init__(N, op, startQubit)
+        if startQubit <= controllingQubit < startQubit + self.getRawOperatorQubitsNumber() or controllingQubit >= N:
+            raise ValueError("the controlling qubit must be outside the operator's qubits")
+        self.ctrlQubit = controllingQubit
+
+    def controls(self) -> list[int]:
+        return [self.ctrlQubit]
+
+    def getNrQubits(self) -> int:
+        return self.nrQubits

@@ -257,6 +257,56 @@ namespace QC {
 				computeGates.emplace_back(Gates::AppliedGate<MatrixClass>(m));
 		}
 
+		// A dense 2^k x 2^k operator U on the target qubits (matrix bit j = qubits[j], k <= 10), applied
+		// where every qubit of ctrlMask is one: the device path of the dense operator gates
+		// (NQubitsQuantumGate.h, NQubitsControlledQuantumGate.h of this directory).  A recording register
+		// applies and logs the 2^n x 2^n extended matrix instead, as the reference's gates do through
+		// ApplyOperatorMatrix (NQubitsQuantumGate.h:20-25).
+		void ApplyOperatorOnQubits(const MatrixClass& U, const std::vector<uint32_t>& qubits, uint64_t ctrlMask = 0)
+		{
+			if (recordGates)
+			{
+				ApplyOperatorMatrix(ExtendedOperator(NrQubits, U, qubits, ctrlMask));
+				return;
+			}
+			std::vector<double> rm(2 * static_cast<size_t>(U.rows()) * static_cast<size_t>(U.cols()));
+			detail::to_row_major(U, rm.data());
+			detail::qcs_check(qcs_apply_operator_on_qubits(handle, rm.data(), static_cast<uint32_t>(qubits.size()), qubits.data(), ctrlMask),
+			                  handle);
+			dirty = true;
+		}
+
+		// the 2^n x 2^n matrix of ApplyOperatorOnQubits on an n-qubit register: U between states that agree
+		// off the targets and have every control set, the identity where a control is clear
+		static MatrixClass ExtendedOperator(size_t n, const MatrixClass& U, const std::vector<uint32_t>& qubits, uint64_t ctrlMask)
+		{
+			const size_t NrBasisStates = 1ULL << n;
+			MatrixClass ext = MatrixClass::Zero(NrBasisStates, NrBasisStates);
+			size_t tmask = 0;
+			for (uint32_t q : qubits) tmask |= 1ULL << q;
+			auto sub = [&](size_t i) {
+				size_t r = 0;
+				for (size_t j = 0; j < qubits.size(); ++j) r |= ((i >> qubits[j]) & 1ULL) << j;
+				return r;
+			};
+			for (size_t i = 0; i < NrBasisStates; ++i)
+			{
+				if ((i & ctrlMask) != ctrlMask)
+				{
+					ext(i, i) = 1;
+					continue;
+				}
+				for (size_t c = 0; c < static_cast<size_t>(U.cols()); ++c)
+				{
+					size_t j = i & ~tmask;
+					for (size_t b = 0; b < qubits.size(); ++b)
+						if ((c >> b) & 1ULL) j |= 1ULL << qubits[b];
+					ext(i, j) = U(sub(i), c);
+				}
+			}
+			return ext;
+		}
+
 		const VectorClass& getRegisterStorage() const
 		{
 			if (dirty || static_cast<size_t>(registerStorage.size()) != NrBasisStates)

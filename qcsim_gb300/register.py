@@ -273,6 +273,20 @@ class QubitRegister:
         if self.recordGates:
             self.computeGates.append(AppliedGate(m.copy()))
 
+    def ApplyOperatorOnQubits(self, m, qubits, controls=()) -> None:
+        """a dense 2^k x 2^k operator (k <= 10) on the given target qubits (matrix bit j = qubits[j]),
+        applied where every control qubit is one: what NQubitsQuantumGate / NQubitsControlledQuantumGate
+        do through their 2^n x 2^n extended matrix (qcs_apply_operator_on_qubits)"""
+        m = np.ascontiguousarray(m, dtype=np.complex128)
+        qs = np.ascontiguousarray(list(qubits), dtype=np.uint32)
+        if m.shape != (1 << qs.size, 1 << qs.size):
+            raise ValueError("operator size does not match the number of target qubits")
+        ctrl = 0
+        for c in controls:
+            ctrl |= 1 << int(c)
+        self._ck(self._lib.qcs_apply_operator_on_qubits(self._h, m.view(np.float64).ctypes.data_as(C.POINTER(C.c_double)),
+                                                        qs.size, qs.ctypes.data_as(C.POINTER(C.c_uint32)), ctrl))
+
     # ---- whole-vector access (QubitRegister.h:507-534) ----
     def getRegisterStorage(self) -> np.ndarray:
         out = np.empty(self.NrBasisStates, dtype=np.complex128)

@@ -23,6 +23,7 @@ bool checkUnitary(const Eigen::MatrixXcd& m)
 #include "GroverAlgorithm.h"
 #include "DraperAdder.h"
 #include "PhaseEstimation.h"
+#include "NQubitsQuantumGate.h"
 
 int main()
 {
@@ -66,5 +67,16 @@ int main()
 	qaoa.Set({ { 0, 1, 1. }, { 1, 2, -1. } }, { 0.1, 0.2, 0.3 });
 	qaoa.SetDeltaE(1.);
 	std::cout << "qaoa energy(3) " << qaoa.Energy(3) << "\n";
+
+	// phase estimation (its controlled powers of U run through NQubitsControlledQuantumGate.h of the
+	// drop-in directory) and a dense operator gate on the top qubits
+	QC::Gates::PhaseShiftGate<> ps(0.75 * 2. * std::acos(-1.));
+	QC::SubAlgo::PhaseEstimation<> pe(ps.getRawOperatorMatrix(), 4, 3);
+	QC::QubitRegister<> per(4);
+	per.setToQubitState(3);
+	std::cout << "phase estimation outcomes " << pe.ExecuteWithMultipleMeasurements(per, 1000).size() << "\n";
+	QC::SubAlgo::NQubitsQuantumGate<> ng(6, Eigen::MatrixXcd::Identity(4, 4), 4);
+	ng.Execute(reg);
+	std::cout << "nqubits extended " << ng.getOperatorMatrix().rows() << "\n";
 	return 0;
 }
