@@ -21,7 +21,8 @@ sample (`cpu_baseline`).
 --impl reference times the CPU oracle (a restatement of QCSim's QubitRegister loops, OpenMP on all
 host threads) on the same workload, a bounded number of gates per step.  Other workloads:
 --config precision (fused FP32 vs FP64 on one circuit), qaoa (512-instance batch, sharded over ranks
-under torchrun), learned (the MLP partition vs greedy vs unfused on an unseen circuit).
+under torchrun), learned (the MLP partition vs greedy vs unfused on an unseen circuit), schrodinger (QCSim's
+split-operator SchrodingerSimulation: Trotter steps/s, with --qubits and --steps).
 """
 from __future__ import annotations
 
@@ -55,7 +56,7 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-gates", type=int, default=60, help="gates in the CPU baseline sample (a third per reference-arm step)")
     ap.add_argument("--model", default=None, help="learned config: cost-model file")
-    ap.add_argument("--config", default="layered", choices=["layered", "precision", "qaoa", "learned"],
+    ap.add_argument("--config", default="layered", choices=["layered", "precision", "qaoa", "learned", "schrodinger"],
                     help="layered: the 30-qubit FP64 circuit (headline); precision: fused FP32 vs plain FP64")
     ap.add_argument("--max-block", type=int, default=3, help="precision config: largest fused block")
     ap.add_argument("--no-fused", action="store_true", help="skip the fused-FP32 comparison in the layered line")
@@ -656,8 +657,72 @@ def run_learned(args):
     print(json.dumps(line))
 
 
+def run_schrodinger(args):
+    """QCSim's SchrodingerSimulation::Execute at full size: a Gaussian packet (2^n grid points) meeting a
+    square barrier, Trotter steps through qcs_schrodinger_evolve.  Reported: device time per step (the
+    potential and kinetic diagonals ride inside the IQFT / QFT shared-memory passes), the wall time of
+    the whole Execute (host operator set-up, uploads and steps), the passes' roofline, and the CPU oracle
+    (its QFT on all host threads) on one step of the same register"""
+    import torch
+    from qcsim_gb300 import _lib as L, circuits
+    from qcsim_gb300.schrodinger import SchrodingerSimulation
+    from oracle import bind as B, schrodinger as OS
+    lib = L.load()
+    n, steps = args.qubits, args.steps
+    nb = 1 << n
+    dt, dx = 0.002, 0.05
+    sim = SchrodingerSimulation(n, dt, dx, steps)
+    stream = torch.cuda.Stream()
+    lib.qcs_set_stream(sim.reg.handle, stream.cuda_stream)
+    sim.setGaussian(nb // 4, nb / 64.0, 20.0)
+    sim.setConstantPotentialInTheMiddle(50.0, nb // 64)
+    psi0 = sim.getRegisterStorage().copy()
+    sim.setNrSteps(args.warmup)
+    sim.Execute()  # warm-up (planning structures, allocations)
+    sim.reg.setRegisterStorageFastNoNormalize(psi0)
+    sim.setNrSteps(steps)
+    torch.cuda.synchronize()
+    sim.reg.profile(True)
+    sim.reg.read_profile()
+    t0 = time.perf_counter()
+    sim.Execute()
+    wall = time.perf_counter() - t0
+    prof = sim.reg.read_profile(fp_ops=True)
+    sim.reg.profile(False)
+    launches, pass_ms, pass_bytes, _ = prof["tile_pass"]
+    step_s = pass_ms / 1e3 / steps
+    peak, peak_kind = peaks()
+    s = 16
+    qb = sum(algorithmic_bytes(op[0], n) for op in circuits.qft_circuit(0, n - 1))
+    alg_step = 2 * qb + 2 * 3 * s * nb  # the two transforms' gates, and two diagonal sweeps (state in and out, table in)
+    norm = float(np.linalg.norm(sim.getRegisterStorage()))
+    # CPU: the oracle's steps (its QFT on all host threads) on the same start state, one step
+    pot, kin = sim.Init()
+    B.build_oracle()
+    c0 = time.perf_counter()
+    OS.evolve_with(psi0 / np.linalg.norm(psi0), n, pot, kin, 1)
+    cpu_s = time.perf_counter() - c0
+    line = {"metric": "Schrodinger split-operator Trotter steps/s", "value": 1.0 / step_s, "unit": "steps/s",
+            "higher_is_better": True, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": f"SchrodingerSimulation, {n} qubits ({nb} grid points), dt {dt}, dx {dx}, Gaussian packet at "
+                                   f"{nb // 4} on a barrier of height 50 and half-width {nb // 64}; {steps} timed steps",
+                       "qubits": n, "steps": steps, "warmup_steps": args.warmup},
+            "ms_per_step": step_s * 1e3, "passes_per_step": launches / steps,
+            "execute_wall_seconds": wall, "norm_after": norm,
+            "roofline": {"bound": "hbm", "achieved": alg_step / step_s / 1e9, "peak": peak, "unit": "GB/s",
+                         "frac": alg_step / step_s / 1e9 / peak, "peak_source": peak_kind,
+                         "algorithmic_bytes_per_step": alg_step,
+                         "pass_GBps": pass_bytes / (pass_ms / 1e3) / 1e9},
+            "cpu_baseline": {"value": 1.0 / cpu_s, "unit": "steps/s", "cores": B.oracle().qo_max_threads(), "kind": "port",
+                             "sample": f"one step of the same {n}-qubit register, {cpu_s:.2f} s"}}
+    print(json.dumps(line))
+
+
 def main():
     args = parse()
+    if args.config == "schrodinger":
+        run_schrodinger(args)
+        return
     if args.config == "precision":
         run_precision(args)
         return

@@ -114,6 +114,15 @@ int qcs_apply_operator_matrix(qcs_handle h, const double* m);
  * qubits qubits[0..k-1] (matrix bit j = qubits[j]), applied to the amplitudes whose control qubits
  * (the set bits of ctrl_mask) are all one; the others are unchanged. */
 int qcs_apply_operator_on_qubits(qcs_handle h, const double* m, uint32_t k, const uint32_t* qubits, uint64_t ctrl_mask);
+/* ApplyOperatorMatrix (QubitRegister.h:499-505) of a diagonal operator: amplitude i *= d[i], d = the
+ * 2^n diagonal entries (interleaved).  QCSim's SchrodingerSimulation applies its potential and kinetic
+ * operators this way (Schrodinger.h:335-347). */
+int qcs_apply_diagonal(qcs_handle h, const double* d);
+/* SchrodingerSimulation::Execute (Schrodinger.h:32-45) after its Init (:291-315): `steps` times the
+ * potential diagonal, the IQFT of the whole register (with the swaps), the kinetic diagonal and the
+ * QFT.  potential_op and kinetic_op are the operators' 2^n diagonal entries (interleaved), sent to the
+ * device once; the diagonals run inside the transforms' shared-memory passes. */
+int qcs_schrodinger_evolve(qcs_handle h, const double* potential_op, const double* kinetic_op, uint64_t steps);
 /* QuantumFourierTransform::QFT / IQFT on qubits [start, end] (QuantumFourierTransform.h:35-87) with
  * the mirror swaps of QubitsSwapper::Swap (QubitsSwapper.h:23-34) when do_swap != 0 */
 int qcs_qft(qcs_handle h, uint32_t start, uint32_t end, int inverse, int do_swap);

@@ -83,6 +83,8 @@ SIGNATURES = {
     "qcs_apply_gates": (_i, [_h, C.c_void_p, _sz]),
     "qcs_apply_operator_matrix": (_i, [_h, _pd]),
     "qcs_apply_operator_on_qubits": (_i, [_h, _pd, _u32, C.POINTER(_u32), _u64]),
+    "qcs_apply_diagonal": (_i, [_h, _pd]),
+    "qcs_schrodinger_evolve": (_i, [_h, _pd, _pd, _u64]),
     "qcs_qft": (_i, [_h, _u32, _u32, _i, _i]),
     "qcs_one_qubit_transform": (_i, [_h, _pd, _u32, _u32, _u32]),
     "qcs_measure_all": (_i, [_h, _d, _pu64]),

@@ -85,7 +85,7 @@ cudaError_t dispatch_one(qcs_handle h, const qcs_gate& g) {
 	if (e != cudaSuccess) return e;
 	h->scale *= c.scale;
 	const double mag = std::abs(h->scale);
-	if (mag > 1e100 || mag < 1e-100) {
+	if (mag > h->scale_limit() || mag < 1.0 / h->scale_limit()) {
 		if (materialize(h) != QCS_OK) return cudaErrorUnknown;
 	}
 	return cudaSuccess;

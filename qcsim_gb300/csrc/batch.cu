@@ -8,6 +8,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <string>
 #include <vector>
 
 #include "batch.cuh"
@@ -18,6 +19,11 @@
 
 namespace qcs {
 namespace {
+
+int fail_cuda(qcs_handle h, cudaError_t e, const char* where) {
+	h->err = std::string(where) + ": " + cudaGetErrorString(e);
+	return QCS_CUDA_ERROR;
+}
 
 qcs_gate make_h(uint32_t q) {
 	qcs_gate g;
@@ -151,6 +157,8 @@ bool op_in_bounds(const TileOp& op, int k, size_t mats) {
 			return false;
 		return op.mat + size_t(4) * D * D <= mats;
 	}
+	if (static_cast<TKind>(op.kind) == TKind::TableDiag)  // every amplitude of the tile, from the table at gtbit
+		return op.nins == 0 && op.lset == 0 && op.gmask == 0 && op.gtbit != 0 && (op.gtbit & 15u) == 0;
 	if (static_cast<TKind>(op.kind) == TKind::PhaseRow) {
 		// lbit1 / lbit2 hold the row's first bit and width; the table covers every z = y << shift
 		const uint32_t shift = op.pad[0], S = op.pad[1], M = op.pad[3];
@@ -191,6 +199,7 @@ double fp_ops_per_item(const TileOp& op) {
 	}
 	switch (kind) {
 	case TKind::PhaseRow: return 8;  // the root from its two table factors, then the amplitude product
+	case TKind::TableDiag: return 4;  // one complex product
 	case TKind::Dense2: return 4 * 16;
 	case TKind::Dense3: return 4 * 64;
 	case TKind::DenseN: return 4.0 * static_cast<double>(1u << (2 * op.nins));
@@ -337,6 +346,9 @@ int run_planned(qcs_handle h, const std::vector<PlannedPass>& passes, int kmax, 
 					tc_slot += 32u * (1u << (2 * c.block_q.size()));
 					tp.dense = 2;
 				}
+			} else if (c.kind == GKind::TableDiag) {
+				op.kind = static_cast<uint8_t>(TKind::TableDiag);
+				op.gtbit = reinterpret_cast<uint64_t>(c.table);
 			} else if (c.kind == GKind::Block) {
 				op.kind = static_cast<uint8_t>(TKind::DenseN);
 				for (uint32_t q : c.block_q) ins.push_back(lpos[q]);
@@ -367,7 +379,7 @@ int run_planned(qcs_handle h, const std::vector<PlannedPass>& passes, int kmax, 
 			return QCS_CUDA_ERROR;
 		}
 		for (uint32_t i = tp.op_begin; i < tp.op_begin + tp.op_count; ++i)
-			if (!op_in_bounds(ops[i], tp.k, mats.size())) {
+			if (!op_in_bounds(ops[i], tp.k, mats.size()) || (tp.dense == 2 && static_cast<TKind>(ops[i].kind) == TKind::TableDiag)) {
 				h->err = "apply gates: internal error (tile operation out of range)";
 				return QCS_CUDA_ERROR;
 			}
@@ -479,7 +491,8 @@ namespace {
 // whose local qubits fit its tile and which shares no qubit with an earlier gate still waiting
 // (gates on disjoint qubits commute), looking at most kGateWindow gates ahead.  The global factors
 // taken out of the gates multiply into the register's scale in placement order; when its magnitude
-// leaves [1e-100, 1e100] the pass closes and the scale is folded into the amplitudes after it.
+// leaves [1/L, L] (L = qcs_register::scale_limit: 1e100 in FP64, 1e15 in FP32) the pass closes and the
+// scale is folded into the amplitudes after it.
 constexpr size_t kGateWindow = 64;
 
 int plan_and_run(qcs_handle h, const std::vector<CompiledGate>& cg, int kmax) {
@@ -510,7 +523,7 @@ int plan_and_run(qcs_handle h, const std::vector<CompiledGate>& cg, int kmax) {
 					pp.gates.push_back(c);
 				}
 				const double mag = std::abs(h->scale);
-				if (mag > 1e100 || mag < 1e-100) {
+				if (mag > h->scale_limit() || mag < 1.0 / h->scale_limit()) {
 					pp.fold_after = h->scale;
 					h->scale = std::complex<double>(1.0, 0.0);
 					fold = true;
@@ -658,6 +671,44 @@ int qft_apply(qcs_handle h, uint32_t start, uint32_t end, bool inverse, bool do_
 		return QCS_OK;
 	}
 	return plan_and_run(h, qft_compiled(start, end, inverse, do_swap), kmax);
+}
+
+// Each step: potential diagonal, IQFT of the whole register (with the swaps), kinetic diagonal, QFT.
+// The diagonals are TableDiag operations, so the planner puts them inside the passes of the
+// neighbouring transforms (no sweep of their own); steps are planned a few at a time.
+int schrodinger_apply(qcs_handle h, const void* d_potential, const void* d_kinetic, uint64_t steps) {
+	const int kmax = h->prec == QCS_FP64 ? tile_qubits<double>() : tile_qubits<float>();
+	const uint32_t end = h->n - 1;
+	CompiledGate pot, kin;
+	pot.kind = kin.kind = GKind::TableDiag;
+	pot.table = d_potential;
+	kin.table = d_kinetic;
+	if (per_gate_mode(h, 2, kmax)) {
+		for (uint64_t s = 0; s < steps; ++s) {
+			cudaError_t e = h->prec == QCS_FP64 ? launch_compiled<double>(static_cast<double2*>(h->d_state), h->N, pot, h->sms, h->stream)
+			                                    : launch_compiled<float>(static_cast<float2*>(h->d_state), h->N, pot, h->sms, h->stream);
+			if (e != cudaSuccess) return fail_cuda(h, e, "schrodinger");
+			if (int st = qft_apply(h, 0, end, true, true)) return st;
+			e = h->prec == QCS_FP64 ? launch_compiled<double>(static_cast<double2*>(h->d_state), h->N, kin, h->sms, h->stream)
+			                        : launch_compiled<float>(static_cast<float2*>(h->d_state), h->N, kin, h->sms, h->stream);
+			if (e != cudaSuccess) return fail_cuda(h, e, "schrodinger");
+			if (int st = qft_apply(h, 0, end, false, true)) return st;
+		}
+		return QCS_OK;
+	}
+	const std::vector<CompiledGate> inv = qft_compiled(0, end, true, true), fwd = qft_compiled(0, end, false, true);
+	constexpr uint64_t kStepsPerPlan = 8;
+	for (uint64_t s0 = 0; s0 < steps; s0 += kStepsPerPlan) {
+		std::vector<CompiledGate> cg;
+		for (uint64_t s = s0; s < std::min(steps, s0 + kStepsPerPlan); ++s) {
+			cg.push_back(pot);
+			cg.insert(cg.end(), inv.begin(), inv.end());
+			cg.push_back(kin);
+			cg.insert(cg.end(), fwd.begin(), fwd.end());
+		}
+		if (int st = plan_and_run(h, cg, kmax)) return st;
+	}
+	return QCS_OK;
 }
 
 void batch_release(qcs_handle h) {

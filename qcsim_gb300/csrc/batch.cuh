@@ -16,6 +16,9 @@ cudaError_t apply_one(qcs_handle h, const qcs_gate& g);
 int batch_apply(qcs_handle h, const qcs_gate* gates, size_t count);
 // QuantumFourierTransform::QFT / IQFT over [start, end]
 int qft_apply(qcs_handle h, uint32_t start, uint32_t end, bool inverse, bool do_swap);
+// SchrodingerSimulation::Execute's Suzuki-Trotter steps (Schrodinger.h:32-45) with its potential and
+// kinetic diagonals already on the device (2^n entries each, the register's precision)
+int schrodinger_apply(qcs_handle h, const void* d_potential, const void* d_kinetic, uint64_t steps);
 void batch_release(qcs_handle h);
 
 // dense blocks applied in shared-memory passes

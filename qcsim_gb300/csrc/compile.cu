@@ -128,6 +128,7 @@ const char* kernel_name(const CompiledGate& c) {
 	case GKind::Dense: return c.dense_k == 2 ? "dense2" : "dense3";
 	case GKind::Block: return "block";
 	case GKind::PhaseRow: return "phase_row";
+	case GKind::TableDiag: return "table_diag";
 	default: return "identity";
 	}
 }
@@ -142,6 +143,7 @@ double touched_fraction(const CompiledGate& c) {
 	case GKind::Dense: return ctl;
 	case GKind::Block: return 1.0;
 	case GKind::PhaseRow: return 0.5;
+	case GKind::TableDiag: return 1.0;
 	default: return 0.0;
 	}
 }
@@ -167,6 +169,7 @@ uint64_t CompiledGate::local_mask() const {
 }
 
 uint64_t CompiledGate::touch_mask() const {
+	if (kind == GKind::TableDiag) return ~0ULL;  // a general diagonal depends on every qubit
 	uint64_t m = local_mask();
 	if (kind == GKind::Ctrl1q) m |= 1ULL << target;
 	if (kind == GKind::PhaseRow) m |= (1ULL << target) | (((1ULL << row_bits) - 1) << row_lo);
@@ -293,6 +296,7 @@ template <typename T> cudaError_t launch_compiled(cplx_t<T>* s, uint64_t N, cons
 		std::memcpy(a.m, c.dense_m, sizeof(a.m));
 		return launch_dense<T>(s, N, a, plan_for(ins, set), sms, st);
 	}
+	case GKind::TableDiag: return launch_table_diag<T>(s, N, static_cast<const cplx_t<T>*>(c.table), sms, st);
 	case GKind::Block:
 	case GKind::PhaseRow: break;  // shared-memory passes only
 	}

@@ -16,7 +16,8 @@ enum class GKind : int {
 	Swap,          // exchange base|bitA with base|bitB, under `controls`
 	Dense,         // 4x4 or 8x8 block on dense_q, under `controls`
 	Block,         // fused block: dense 2^m x 2^m matrix on block_q (ascending), no controls
-	PhaseRow       // the QFT's run of controlled phases on one target (see below); shared-memory passes only
+	PhaseRow,      // the QFT's run of controlled phases on one target (see below); shared-memory passes only
+	TableDiag      // diagonal operator from a device table: amplitude i *= table[i] (table in the register's precision)
 };
 
 struct CompiledGate {
@@ -41,6 +42,7 @@ struct CompiledGate {
 	// over controls c = target - 1 .. row_lo, the phases one QFT step applies to one target
 	uint32_t row_lo = 0, row_bits = 0;
 	bool row_inverse = false;
+	const void* table = nullptr;  // TableDiag: 2^n entries on the device
 
 	// qubits whose bit a tile must hold locally to apply this gate (targets of non-diagonal blocks)
 	uint64_t local_mask() const;
@@ -60,5 +62,9 @@ template <typename T> cudaError_t launch_compiled(cplx_t<T>* s, uint64_t N, cons
 
 template <typename T>
 cudaError_t launch_scale_complex(cplx_t<T>* s, uint64_t N, double re, double im, int sms, cudaStream_t st);
+
+// amplitude i *= d[i] over the whole register (operator.cu)
+template <typename T>
+cudaError_t launch_table_diag(cplx_t<T>* s, uint64_t N, const cplx_t<T>* d, int sms, cudaStream_t st);
 
 }  // namespace qcs

@@ -101,6 +101,9 @@ struct qcs_register {
 	void* prof = nullptr;                  // launch timing records (profile.cu), when enabled
 	std::string err;
 	size_t amp_bytes() const { return prec == QCS_FP64 ? 16 : 8; }
+	// the pending factor is folded into the amplitudes once its magnitude leaves [1/limit, limit], so that
+	// stored values (amplitude / scale) stay far inside the precision's range
+	double scale_limit() const { return prec == QCS_FP64 ? 1e100 : 1e15; }
 	size_t state_bytes() const { return static_cast<size_t>(N) * amp_bytes(); }
 };
 

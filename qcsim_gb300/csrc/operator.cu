@@ -16,7 +16,10 @@
 #include <string>
 #include <vector>
 
+#include "batch.cuh"
+#include "compile.cuh"
 #include "engine.cuh"
+#include "gate_math.cuh"
 
 namespace qcs {
 namespace {
@@ -146,8 +149,79 @@ int apply(qcs_handle h, const double* m, uint32_t k, const OpGeom& geo, uint64_t
 	return QCS_OK;
 }
 
+// a diagonal operator's entries on the device, in the register's precision (cudaMallocAsync on the
+// register's stream; release with cudaFreeAsync on the same stream)
+template <typename T>
+cudaError_t upload_diagonal(qcs_handle h, const double* d, void** out) {
+	std::vector<cplx_t<T>> v(h->N);
+	for (uint64_t i = 0; i < h->N; ++i) {
+		v[i].x = static_cast<T>(d[2 * i]);
+		v[i].y = static_cast<T>(d[2 * i + 1]);
+	}
+	cudaError_t e = cudaMallocAsync(out, v.size() * sizeof(cplx_t<T>), h->stream);
+	if (e != cudaSuccess) return e;
+	// pageable source: the call returns once the entries are staged
+	return cudaMemcpyAsync(*out, v.data(), v.size() * sizeof(cplx_t<T>), cudaMemcpyHostToDevice, h->stream);
+}
+
+cudaError_t upload_diagonal_any(qcs_handle h, const double* d, void** out) {
+	return h->prec == QCS_FP64 ? upload_diagonal<double>(h, d, out) : upload_diagonal<float>(h, d, out);
+}
+
 }  // namespace
+
+template <typename T>
+__global__ void k_table_diag(cplx_t<T>* __restrict__ s, const cplx_t<T>* __restrict__ d, uint64_t N) {
+	const uint64_t stride = static_cast<uint64_t>(gridDim.x) * blockDim.x;
+	for (uint64_t i = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < N; i += stride) s[i] = cmul<T>(s[i], d[i]);
+}
+
+template <typename T>
+cudaError_t launch_table_diag(cplx_t<T>* s, uint64_t N, const cplx_t<T>* d, int sms, cudaStream_t st) {
+	k_table_diag<T><<<grid_for(N, 256, sms), 256, 0, st>>>(s, d, N);
+	note_launches(1);
+	return cudaGetLastError();
+}
+template cudaError_t launch_table_diag<double>(double2*, uint64_t, const double2*, int, cudaStream_t);
+template cudaError_t launch_table_diag<float>(float2*, uint64_t, const float2*, int, cudaStream_t);
+
 }  // namespace qcs
+
+extern "C" int qcs_apply_diagonal(qcs_handle h, const double* d) {
+	if (!h || !d) return QCS_INVALID_ARGUMENT;
+	void* dd = nullptr;
+	cudaError_t e = qcs::upload_diagonal_any(h, d, &dd);
+	if (e == cudaSuccess) {
+		qcs::prof_begin(h, "table_diag", 3.0 * h->amp_bytes() * static_cast<double>(h->N));
+		e = h->prec == QCS_FP64
+		        ? qcs::launch_table_diag<double>(static_cast<double2*>(h->d_state), h->N, static_cast<const double2*>(dd), h->sms, h->stream)
+		        : qcs::launch_table_diag<float>(static_cast<float2*>(h->d_state), h->N, static_cast<const float2*>(dd), h->sms, h->stream);
+		qcs::prof_end(h);
+	}
+	if (dd) {
+		const cudaError_t ef = cudaFreeAsync(dd, h->stream);
+		if (e == cudaSuccess) e = ef;
+	}
+	if (e != cudaSuccess) return qcs::cuda_fail(h, e, "diagonal operator");
+	return QCS_OK;
+}
+
+extern "C" int qcs_schrodinger_evolve(qcs_handle h, const double* potential_op, const double* kinetic_op, uint64_t steps) {
+	if (!h || !potential_op || !kinetic_op) return QCS_INVALID_ARGUMENT;
+	void *dv = nullptr, *dk = nullptr;
+	cudaError_t e = qcs::upload_diagonal_any(h, potential_op, &dv);
+	if (e == cudaSuccess) e = qcs::upload_diagonal_any(h, kinetic_op, &dk);
+	int st = QCS_OK;
+	if (e == cudaSuccess) st = qcs::schrodinger_apply(h, dv, dk, steps);
+	for (void* p : {dv, dk})
+		if (p) {
+			const cudaError_t ef = cudaFreeAsync(p, h->stream);
+			if (e == cudaSuccess) e = ef;
+		}
+	if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+	if (e != cudaSuccess) return qcs::cuda_fail(h, e, "schrodinger");
+	return st;
+}
 
 extern "C" int qcs_apply_operator_on_qubits(qcs_handle h, const double* m, uint32_t k, const uint32_t* qubits, uint64_t ctrl_mask) {
 	if (!h || !m || !qubits) return QCS_INVALID_ARGUMENT;

@@ -16,7 +16,10 @@ namespace qcs {
 // mat = offset (complex entries, even) of its real-expanded 2D x 2D matrix as two TF32 splits in the
 // K-major operand layout (hi then lo, 16 D^2 bytes each), lbit1 = its byte offset in the kernel's
 // resident matrix area
-enum class TKind : uint8_t { Ctrl1q = 0, Swap = 1, Dense2 = 2, Dense3 = 3, GlobalDiag = 4, DenseN = 5, PhaseRow = 6, DenseTC = 7 };
+// TableDiag: every amplitude of the tile times its entry of a 2^n-entry diagonal on the device (the
+// table's address in gtbit); no inserted positions
+enum class TKind : uint8_t { Ctrl1q = 0, Swap = 1, Dense2 = 2, Dense3 = 3, GlobalDiag = 4, DenseN = 5, PhaseRow = 6, DenseTC = 7,
+                             TableDiag = 8 };
 
 // tensor-core passes: tiles of exactly kTcTileQubits qubits; resident block matrices per pass
 constexpr int kTcTileQubits = 12;
@@ -35,7 +38,7 @@ struct TileOp {
 	uint32_t lbit2;    // Dense3: matrix bit 2
 	uint32_t mat;      // offset of the op's entries in the pass matrix table (complex entries)
 	uint64_t gmask;    // non-tile controls: the op applies only in tiles whose fixed bits include these
-	uint64_t gtbit;    // GlobalDiag: the non-tile target bit selecting m00 (clear) or m11 (set)
+	uint64_t gtbit;    // GlobalDiag: the non-tile target bit selecting m00 (clear) or m11 (set); TableDiag: the table's address
 };
 
 // per-pass geometry

@@ -380,7 +380,12 @@ __global__ void __launch_bounds__(THREADS) k_tile(cplx_t<T>* __restrict__ s, Til
 		for (uint32_t oi = 0; oi < p.op_count; ++oi) {
 			const TileOp op = opsrc[oi];
 			if ((base & op.gmask) != op.gmask) continue;
-			tile_apply<T, DENSE>(sm, p.k, op, mats, base, highoff, p.L);
+			if (static_cast<TKind>(op.kind) == TKind::TableDiag) {
+				const cplx_t<T>* tab = reinterpret_cast<const cplx_t<T>*>(op.gtbit);
+				for (uint32_t j = threadIdx.x; j < K; j += blockDim.x) sm[j] = cmul<T>(sm[j], tab[base | highoff[j >> p.L] | (j & lowmask)]);
+			} else {
+				tile_apply<T, DENSE>(sm, p.k, op, mats, base, highoff, p.L);
+			}
 			__syncthreads();
 		}
 		for (uint32_t j0 = threadIdx.x; j0 < K; j0 += blockDim.x * load_batch<T>()) {

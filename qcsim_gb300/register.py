@@ -268,10 +268,26 @@ class QubitRegister:
         self._ck(self._lib.qcs_apply_gates(self._h, recs.ctypes.data_as(C.c_void_p), len(recs)))
 
     def ApplyOperatorMatrix(self, m) -> None:
+        """ApplyOperatorMatrix (QubitRegister.h:499-505): a dense 2^n x 2^n operator; a diagonal one (every
+        non-zero entry on the diagonal) runs as one multiply per amplitude (qcs_apply_diagonal)"""
         m = np.ascontiguousarray(m, dtype=np.complex128)
-        self._ck(self._lib.qcs_apply_operator_matrix(self._h, m.view(np.float64).ctypes.data_as(C.POINTER(C.c_double))))
+        N = self.getNrBasisStates()
+        if m.shape != (N, N):
+            raise ValueError("the operator must be 2^n x 2^n")
+        d = np.ascontiguousarray(np.diagonal(m))
+        if np.count_nonzero(m) == np.count_nonzero(d):
+            self._ck(self._lib.qcs_apply_diagonal(self._h, d.view(np.float64).ctypes.data_as(C.POINTER(C.c_double))))
+        else:
+            self._ck(self._lib.qcs_apply_operator_matrix(self._h, m.view(np.float64).ctypes.data_as(C.POINTER(C.c_double))))
         if self.recordGates:
             self.computeGates.append(AppliedGate(m.copy()))
+
+    def ApplyDiagonal(self, d) -> None:
+        """amplitude i *= d[i] for the 2^n entries d (qcs_apply_diagonal), without a 2^n x 2^n matrix"""
+        d = np.ascontiguousarray(d, dtype=np.complex128)
+        if d.shape != (self.getNrBasisStates(),):
+            raise ValueError("the diagonal must have 2^n entries")
+        self._ck(self._lib.qcs_apply_diagonal(self._h, d.view(np.float64).ctypes.data_as(C.POINTER(C.c_double))))
 
     def ApplyOperatorOnQubits(self, m, qubits, controls=()) -> None:
         """a dense 2^k x 2^k operator (k <= 10) on the given target qubits (matrix bit j = qubits[j]),

@@ -528,3 +528,26 @@ def test_pass_fp_op_count(Q):
     launches, _, _, ops = prof["tile_pass"]
     assert launches == 1 and ops == 6 * N, (launches, ops)
     reg.close()
+
+
+@pytest.mark.parametrize("batched", [False, True])
+def test_fp32_long_factored_sequences(Q, batched):
+    """600 Hadamards on one qubit of an FP32 register (each leaves a factor 1/sqrt(2) pending): the
+    pending factor is folded before the stored values leave FP32's range, and H^600 = identity"""
+    from qcsim_gb300 import gates as G
+    n = 16
+    rng = np.random.default_rng(3)
+    v = rng.standard_normal(1 << n) + 1j * rng.standard_normal(1 << n)
+    v /= np.linalg.norm(v)
+    reg = Q.QubitRegister(n, seed=1, precision="fp32")
+    reg.setRegisterStorageFastNoNormalize(v)
+    ops = [(G.HadamardGate(), 3)] * 600
+    if batched:
+        reg.ApplyGates(ops)
+    else:
+        for g, q in ops:
+            reg.ApplyGate(g, q)
+    got = reg.getRegisterStorage()
+    assert np.all(np.isfinite(got.view(np.float32)))
+    assert np.abs(got - v).max() < 1e-5
+    reg.close()
