@@ -74,8 +74,18 @@ struct BatchBuffers {
 	size_t ops_cap = 0;
 	void* d_mats = nullptr;
 	size_t mats_cap = 0;
-	int* d_err = nullptr;  // status word of the tensor-core passes
+	int* d_err = nullptr;     // status word of the tensor-core passes
+	void* d_roots = nullptr;  // all 2^roots_M-th roots of unity for the phase rows (0: none built)
+	uint32_t roots_M = 0;
 };
+
+// phase rows of at most kRootsM - 1 bits read their root from one table of 2^kRootsM entries (4 FP64
+// operations per amplitude fewer than combining two factors); 2^24 complex doubles = 256 MiB
+constexpr uint32_t kRootsM = 24;
+
+// QFT rows narrower than this stay individual controlled phases (a row costs one or two complex products
+// on half the amplitudes; a controlled phase one product on a quarter)
+constexpr uint32_t kMinRowBits = 5;
 
 cudaError_t ensure(void** p, size_t* cap, size_t bytes) {
 	if (*cap >= bytes) return cudaSuccess;
@@ -164,6 +174,7 @@ bool op_in_bounds(const TileOp& op, int k, size_t mats) {
 		const uint32_t shift = op.pad[0], S = op.pad[1], M = op.pad[3];
 		if (op.nins > 1 || op.lbit0 != 0 || M < 1 || M > 40 || S > M || op.lbit1 + op.lbit2 > 64 || op.lbit2 + shift > M)
 			return false;
+		if (op.pad[4]) return M <= kRootsM && op.gtbit != 0 && (op.gtbit & 15u) == 0;  // the full table: 2^M entries
 		return op.mat + (size_t(1) << (M - S)) + (size_t(1) << S) <= mats;
 	}
 	const bool flag0 = static_cast<TKind>(op.kind) == TKind::GlobalDiag;  // lbit0 is a side flag there
@@ -198,7 +209,7 @@ double fp_ops_per_item(const TileOp& op) {
 		}
 	}
 	switch (kind) {
-	case TKind::PhaseRow: return 8;  // the root from its two table factors, then the amplitude product
+	case TKind::PhaseRow: return op.pad[4] ? 4 : 8;  // the root from the full table or from two factors, then the product
 	case TKind::TableDiag: return 4;  // one complex product
 	case TKind::Dense2: return 4 * 16;
 	case TKind::Dense3: return 4 * 64;
@@ -372,6 +383,36 @@ int run_planned(qcs_handle h, const std::vector<PlannedPass>& passes, int kmax, 
 		tp.op_count = static_cast<uint32_t>(ops.size()) - tp.op_begin;
 		tps.push_back(tp);
 	}
+	BatchBuffers* bb = static_cast<BatchBuffers*>(h->batch);
+	if (!bb) {
+		bb = new BatchBuffers;
+		h->batch = bb;
+	}
+	// rows narrow enough for the full table of 2^M0 roots read it (z = y << (M0 - 1 - bits)); it is built
+	// on the device from the two-level tables once per register and size
+	const uint32_t M0 = std::min(rowM, kRootsM);
+	bool build_roots = false;
+	if (rowM > 0 && M0 >= kMinRowBits + 1) {
+		if (bb->roots_M != M0) {
+			if (bb->d_roots) cudaFree(bb->d_roots);
+			bb->d_roots = nullptr;
+			bb->roots_M = 0;
+			if (cudaMalloc(&bb->d_roots, (size_t(1) << M0) * sizeof(cplx_t<T>)) == cudaSuccess) {
+				bb->roots_M = M0;
+				build_roots = true;
+			} else {
+				cudaGetLastError();  // no room: the rows keep the two-level form
+			}
+		}
+		if (bb->roots_M == M0)
+			for (TileOp& op : ops)
+				if (static_cast<TKind>(op.kind) == TKind::PhaseRow && op.lbit2 + 1 <= M0) {
+					op.pad[0] = static_cast<uint8_t>(M0 - 1 - op.lbit2);
+					op.pad[3] = static_cast<uint8_t>(M0);
+					op.pad[4] = 1;
+					op.gtbit = reinterpret_cast<uint64_t>(bb->d_roots);
+				}
+	}
 	// every index a kernel will form stays inside its tile and every matrix read inside the table
 	for (const TilePass& tp : tps) {
 		if (tp.k < 1 || tp.k > tile_qubits<T>() || tp.L > tp.k || tp.k - tp.L > 8 || tp.nfixed + tp.k != n) {
@@ -379,15 +420,12 @@ int run_planned(qcs_handle h, const std::vector<PlannedPass>& passes, int kmax, 
 			return QCS_CUDA_ERROR;
 		}
 		for (uint32_t i = tp.op_begin; i < tp.op_begin + tp.op_count; ++i)
-			if (!op_in_bounds(ops[i], tp.k, mats.size()) || (tp.dense == 2 && static_cast<TKind>(ops[i].kind) == TKind::TableDiag)) {
+			if (!op_in_bounds(ops[i], tp.k, mats.size()) || (tp.dense == 2 && static_cast<TKind>(ops[i].kind) == TKind::TableDiag) ||
+			    (static_cast<TKind>(ops[i].kind) == TKind::PhaseRow && ops[i].pad[4] &&
+			     (ops[i].pad[3] != bb->roots_M || ops[i].gtbit != reinterpret_cast<uint64_t>(bb->d_roots)))) {
 				h->err = "apply gates: internal error (tile operation out of range)";
 				return QCS_CUDA_ERROR;
 			}
-	}
-	BatchBuffers* bb = static_cast<BatchBuffers*>(h->batch);
-	if (!bb) {
-		bb = new BatchBuffers;
-		h->batch = bb;
 	}
 	cudaError_t e = ensure(&bb->d_ops, &bb->ops_cap, std::max<size_t>(1, ops.size()) * sizeof(TileOp));
 	if (e == cudaSuccess) e = ensure(&bb->d_mats, &bb->mats_cap, std::max<size_t>(1, mats.size()) * sizeof(cplx_t<T>));
@@ -395,6 +433,31 @@ int run_planned(qcs_handle h, const std::vector<PlannedPass>& passes, int kmax, 
 		e = cudaMemcpyAsync(bb->d_ops, ops.data(), ops.size() * sizeof(TileOp), cudaMemcpyHostToDevice, h->stream);
 	if (e == cudaSuccess && !mats.empty())
 		e = cudaMemcpyAsync(bb->d_mats, mats.data(), mats.size() * sizeof(cplx_t<T>), cudaMemcpyHostToDevice, h->stream);
+	if (e == cudaSuccess && build_roots) {
+		// the two-level tables of size M0: the first row table's entries were built for rowM, so the
+		// full table gets its own pair, computed here on the host the same way
+		std::vector<cplx_t<T>> pair;
+		const uint32_t S0 = (M0 + 1) / 2;
+		for (uint64_t u = 0; u < (1ULL << (M0 - S0)); ++u) {
+			const double a = 2.0 * M_PI * std::ldexp(static_cast<double>(u), static_cast<int>(S0) - static_cast<int>(M0));
+			pair.push_back(mk_host<T>(std::cos(a), std::sin(a)));
+		}
+		for (uint64_t v = 0; v < (1ULL << S0); ++v) {
+			const double a = 2.0 * M_PI * std::ldexp(static_cast<double>(v), -static_cast<int>(M0));
+			pair.push_back(mk_host<T>(std::cos(a), std::sin(a)));
+		}
+		void* d_pair = nullptr;
+		e = cudaMallocAsync(&d_pair, pair.size() * sizeof(cplx_t<T>), h->stream);
+		if (e == cudaSuccess) e = cudaMemcpyAsync(d_pair, pair.data(), pair.size() * sizeof(cplx_t<T>), cudaMemcpyHostToDevice, h->stream);
+		if (e == cudaSuccess)
+			e = launch_build_roots<T>(static_cast<cplx_t<T>*>(bb->d_roots), static_cast<const cplx_t<T>*>(d_pair), M0, S0, h->sms, h->stream);
+		if (d_pair) {
+			const cudaError_t ef = cudaFreeAsync(d_pair, h->stream);
+			if (e == cudaSuccess) e = ef;
+		}
+		if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);  // the host pair must outlive its copy
+		if (e != cudaSuccess) bb->roots_M = 0;
+	}
 	bool any_tc = false;
 	for (const TilePass& tp : tps) any_tc = any_tc || tp.dense == 2;
 	if (e == cudaSuccess && any_tc && !bb->d_err) e = cudaMalloc(&bb->d_err, sizeof(int));
@@ -604,9 +667,6 @@ std::vector<qcs_gate> qft_gates(uint32_t start, uint32_t end, bool inverse, bool
 
 namespace {
 
-// QFT rows narrower than this stay individual controlled phases (a row costs two complex products on
-// half the amplitudes; a controlled phase one product on a quarter)
-constexpr uint32_t kMinRowBits = 5;
 
 // the QFT's gate sequence with each target's run of controlled phases as one PhaseRow: the phases
 // commute (all diagonal) and sit between the same two Hadamards, so their product is applied at once
@@ -717,6 +777,7 @@ void batch_release(qcs_handle h) {
 	if (bb->d_ops) cudaFree(bb->d_ops);
 	if (bb->d_mats) cudaFree(bb->d_mats);
 	if (bb->d_err) cudaFree(bb->d_err);
+	if (bb->d_roots) cudaFree(bb->d_roots);
 	delete bb;
 	h->batch = nullptr;
 }

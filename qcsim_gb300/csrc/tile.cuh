@@ -11,7 +11,8 @@ namespace qcs {
 // DenseN: a fused block's 2^nins x 2^nins matrix whose bit j is the j-th inserted position
 // PhaseRow: a QFT phase row (CompiledGate::PhaseRow): lbit1 = row_lo, lbit2 = row_bits, pad[0] = the
 // shift taking y to the table's 2^M-th roots, pad[1] = S, pad[2] = inverse, pad[3] = M; the factor
-// exp(2 pi i z / 2^M), z = y << shift, is table[mat + (z >> S)] * table[mat + 2^(M-S) + (z & (2^S - 1))]
+// exp(2 pi i z / 2^M), z = y << shift, is table[mat + (z >> S)] * table[mat + 2^(M-S) + (z & (2^S - 1))];
+// with pad[4] = 1 it is full[z] instead, from a table of all 2^M roots at address gtbit
 // DenseTC: a fused 4- or 5-qubit block (FP32 registers) on the tensor cores; ins = its local positions,
 // mat = offset (complex entries, even) of its real-expanded 2D x 2D matrix as two TF32 splits in the
 // K-major operand layout (hi then lo, 16 D^2 bytes each), lbit1 = its byte offset in the kernel's
@@ -57,6 +58,11 @@ struct TilePass {
 template <typename T>
 cudaError_t launch_tile_pass(cplx_t<T>* s, const TilePass& p, const TileOp* d_ops, const cplx_t<T>* d_mats, int sms,
                              cudaStream_t st, int* d_err);
+
+// full[z] = hilo[z >> S] * hilo[2^(M-S) + (z & (2^S - 1))] for z < 2^M: every 2^M-th root of unity, from the
+// two-level tables of the phase rows (the same products the two-level form computes per amplitude)
+template <typename T>
+cudaError_t launch_build_roots(cplx_t<T>* full, const cplx_t<T>* hilo, uint32_t M, uint32_t S, int sms, cudaStream_t st);
 
 // largest tile (qubits) for the precision, given the shared memory per block
 template <typename T> int tile_qubits();

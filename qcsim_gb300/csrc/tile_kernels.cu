@@ -182,12 +182,13 @@ __device__ __forceinline__ void tile_phaserow(cplx_t<T>* sm, uint32_t items, con
 	const uint64_t ymask = (1ULL << row_bits) - 1, smask = (1ULL << S) - 1;
 	const cplx_t<T>* hi = mats + op.mat;
 	const cplx_t<T>* lo = hi + (1ULL << (M - S));
+	const cplx_t<T>* full = top.pad[4] ? reinterpret_cast<const cplx_t<T>*>(top.gtbit) : nullptr;
 	const uint32_t lowmask = (1u << L) - 1;
 	for (uint32_t i = threadIdx.x; i < items; i += blockDim.x) {
 		const uint32_t b = expand_local(i, op);
 		const uint64_t g = base | highoff[b >> L] | (b & lowmask);
 		const uint64_t z = ((g >> row_lo) & ymask) << shift;
-		cplx_t<T> w = cmul<T>(hi[z >> S], lo[z & smask]);
+		cplx_t<T> w = full ? full[z] : cmul<T>(hi[z >> S], lo[z & smask]);
 		if (inverse) w.y = -w.y;
 		sm[b] = cmul<T>(sm[b], w);
 	}
@@ -341,6 +342,14 @@ __device__ __forceinline__ void tile_apply(cplx_t<T>* sm, int k, const TileOp& t
 		default: tile_denseN<T, 4>(sm, items, op, mats); break;
 		}
 	}
+}
+
+template <typename T>
+__global__ void k_build_roots(cplx_t<T>* __restrict__ full, const cplx_t<T>* __restrict__ hilo, uint32_t M, uint32_t S) {
+	const uint64_t n = 1ULL << M, smask = (1ULL << S) - 1;
+	const cplx_t<T>* lo = hilo + (1ULL << (M - S));
+	for (uint64_t z = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x; z < n; z += static_cast<uint64_t>(gridDim.x) * blockDim.x)
+		full[z] = cmul<T>(hilo[z >> S], lo[z & smask]);
 }
 
 template <typename T, bool DENSE, int THREADS>
@@ -772,5 +781,14 @@ cudaError_t launch_tile_pass(cplx_t<T>* s, const TilePass& p, const TileOp* d_op
 
 template cudaError_t launch_tile_pass<double>(double2*, const TilePass&, const TileOp*, const double2*, int, cudaStream_t, int*);
 template cudaError_t launch_tile_pass<float>(float2*, const TilePass&, const TileOp*, const float2*, int, cudaStream_t, int*);
+
+template <typename T>
+cudaError_t launch_build_roots(cplx_t<T>* full, const cplx_t<T>* hilo, uint32_t M, uint32_t S, int sms, cudaStream_t st) {
+	k_build_roots<T><<<grid_for(1ULL << M, 256, sms), 256, 0, st>>>(full, hilo, M, S);
+	note_launches(1);
+	return cudaGetLastError();
+}
+template cudaError_t launch_build_roots<double>(double2*, const double2*, uint32_t, uint32_t, int, cudaStream_t);
+template cudaError_t launch_build_roots<float>(float2*, const float2*, uint32_t, uint32_t, int, cudaStream_t);
 
 }  // namespace qcs
