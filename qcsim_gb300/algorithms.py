@@ -1,8 +1,10 @@
-"""Sub-algorithms of the hot path, mirroring QCSim's QC::SubAlgo classes over the engine:
+"""Algorithms of the hot path, mirroring QCSim's classes over the engine: the QC::QuantumAlgorithm base
+(QuantumAlgorithm.h:9-205), the QC::SubAlgo classes
 QuantumFourierTransform (QuantumFourierTransform.h:12-92), QubitsSwapper (QubitsSwapper.h:10-43),
-OneQubitGateTransform / HadamardTransform / XTransform (HadamardTransform.h:9-41), and the dense
-operator gates NQubitsQuantumGate (NQubitsQuantumGate.h:9-78) / NQubitsControlledQuantumGate
-(NQubitsControlledQuantumGate.h:9-97).
+OneQubitGateTransform / HadamardTransform / XTransform (HadamardTransform.h:9-41), the dense operator
+gates NQubitsQuantumGate (NQubitsQuantumGate.h:9-78) / NQubitsControlledQuantumGate
+(NQubitsControlledQuantumGate.h:9-97), phase estimation (PhaseEstimation.h:11-231) and Grover's search
+with the diagonal oracle matrix (GroverAlgorithm.h:14-124).
 
 The QFT runs as one engine call (qcs_qft), which applies the reference's gate sequence; the one-qubit
 transforms run as one gate list (qcs_one_qubit_transform); the dense operator gates run as one
@@ -11,10 +13,12 @@ qcs_apply_operator_on_qubits call on their 2^k x 2^k operator.
 from __future__ import annotations
 
 import ctypes as C
+import math
 
 import numpy as np
 
 from . import gates as G
+from .register import QubitRegister
 
 INT_MAX = 2**31 - 1
 
@@ -182,3 +186,243 @@ class NQubitsControlledQuantumGate(NQubitsQuantumGate):
 
     def getNrQubits(self) -> int:
         return self.nrQubits
+
+
+class QuantumAlgorithm:
+    """QC::QuantumAlgorithm (QuantumAlgorithm.h:9-205): owns the register and forwards the state setters,
+    gates, measurements and record / replay to it"""
+
+    def __init__(self, N: int = 3, addseed: int = 0, *, precision: str = "fp64", seed: int | None = None):
+        self.reg = QubitRegister(N, addseed, precision=precision, seed=seed)
+
+    def getNrQubits(self) -> int:
+        return self.reg.getNrQubits()
+
+    def getNrBasisStates(self) -> int:
+        return self.reg.getNrBasisStates()
+
+    def getBasisStateAmplitude(self, State: int) -> complex:
+        return self.reg.getBasisStateAmplitude(State)
+
+    def getBasisStateProbability(self, State: int) -> float:
+        return self.reg.getBasisStateProbability(State)
+
+    def setToBasisState(self, State: int) -> None:
+        self.reg.setToBasisState(State)
+
+    def setToQubitState(self, q: int) -> None:
+        self.reg.setToQubitState(q)
+
+    def setToCatState(self) -> None:
+        self.reg.setToCatState()
+
+    def setToEqualSuperposition(self) -> None:
+        self.reg.setToEqualSuperposition()
+
+    def setRawAmplitude(self, State: int, val: complex) -> None:
+        self.reg.setRawAmplitude(State, val)
+
+    def Clear(self) -> None:
+        self.reg.Clear()
+
+    def Normalize(self) -> None:
+        self.reg.Normalize()
+
+    def AdjustPhaseAndNormalize(self) -> None:
+        self.reg.AdjustPhaseAndNormalize()
+
+    def getRegister(self) -> QubitRegister:
+        return self.reg
+
+    def getRegisterStorage(self) -> np.ndarray:
+        return self.reg.getRegisterStorage()
+
+    def setRegisterStorage(self, vals) -> None:
+        self.reg.setRegisterStorage(vals)
+
+    def ApplyGate(self, gate, qubit=None, controllingQubit: int = 0, controllingQubit2: int = 0) -> None:
+        self.reg.ApplyGate(gate, qubit, controllingQubit, controllingQubit2)
+
+    def ApplyGates(self, gates) -> None:
+        self.reg.ApplyGates(gates)
+
+    def ApplyOperatorMatrix(self, m) -> None:
+        self.reg.ApplyOperatorMatrix(m)
+
+    def RepeatedMeasure(self, *args) -> dict:
+        return self.reg.RepeatedMeasure(*args)
+
+    def Measure(self, *args) -> int:
+        """Measure() = MeasureAll, Measure(q) = MeasureQubit, Measure(first, second) (QuantumAlgorithm.h:121-135)"""
+        if not args:
+            return self.reg.MeasureAll()
+        if len(args) == 1:
+            return self.reg.MeasureQubit(args[0])
+        return self.reg.Measure(args[0], args[1])
+
+    def stateFidelity(self, state) -> float:
+        return self.reg.stateFidelity(state)
+
+    def ComputeStart(self) -> None:
+        self.reg.ComputeStart()
+
+    def ComputeEnd(self) -> None:
+        self.reg.ComputeEnd()
+
+    def ComputeClear(self) -> None:
+        self.reg.ComputeClear()
+
+    def Compute(self) -> None:
+        self.reg.Compute()
+
+    def Uncompute(self) -> None:
+        self.reg.Uncompute()
+
+    def close(self) -> None:
+        self.reg.close()
+
+
+class PhaseEstimationBase:
+    """SubAlgo::PhaseEstimationBase (PhaseEstimation.h:11-100): an L-qubit x register (qubits 0 .. L-1) and
+    the function register above it"""
+
+    def __init__(self, N: int = 7, L: int = 3):
+        self.fRegisterStartQubit = L
+        self.nrQubits = N
+        self.fourier = QuantumFourierTransform(N, 0, L - 1)
+
+    def getFunctionStartQubit(self) -> int:
+        return self.fRegisterStartQubit
+
+    def getNrQubits(self) -> int:
+        return self.nrQubits
+
+    def getPhase(self, mostMeasuredState: int, secondMostMeasuredState: int, estimatedProbability: float,
+                 nrSteps: int = 10000) -> float:
+        """the phase from the two most frequent outcomes (PhaseEstimation.h:32-66): the offset phi whose
+        ideal peak probability is closest to the measured one"""
+        nrStates = 1 << self.fRegisterStartQubit
+        if secondMostMeasuredState == -1:
+            return mostMeasuredState / nrStates
+        p, phi = 1.0, 0.0
+        pref = 1.0 / float(1 << (2 * self.fRegisterStartQubit))
+        prefe = 2.0 * math.pi * 1j
+        for i in range(1, nrSteps):
+            curPhi = i / nrSteps
+            e = prefe * curPhi
+            a = (np.exp(e) - 1.0) / (np.exp(e / nrStates) - 1.0)
+            curProb = pref * abs(a) ** 2
+            if abs(estimatedProbability - curProb) < abs(estimatedProbability - p):
+                p, phi = curProb, curPhi
+        if mostMeasuredState != 0:
+            if mostMeasuredState < secondMostMeasuredState and secondMostMeasuredState != nrStates - 1:
+                return (mostMeasuredState + phi) / nrStates
+            if mostMeasuredState > secondMostMeasuredState:
+                return (mostMeasuredState - phi) / nrStates
+        return 1.0 + (mostMeasuredState - phi) / nrStates
+
+    def Init(self, reg) -> None:
+        """the function register's lowest qubit set, Hadamards on the x register (PhaseEstimation.h:69-87)"""
+        reg.setToQubitState(self.fRegisterStartQubit)
+        self.ApplyHadamardOnXRegister(reg)
+
+    def ApplyHadamardOnXRegister(self, reg) -> None:
+        for i in range(self.fRegisterStartQubit):
+            reg.ApplyGate(self.fourier.hadamard, i)
+
+    def IQFT(self, reg, swap: bool = True) -> None:
+        self.fourier.IQFT(reg, swap)
+
+
+class PhaseEstimation(PhaseEstimationBase):
+    """SubAlgo::PhaseEstimation (PhaseEstimation.h:153-231): the controlled powers U^(2^j) as
+    NQubitsControlledQuantumGate (on the device, no extended matrix), then the IQFT without swaps"""
+
+    def __init__(self, op, N: int = 7, L: int = 3):
+        super().__init__(N, L)
+        self.U = np.array(op, dtype=np.complex128)
+        if self.U.shape[0] != self.U.shape[1]:
+            raise ValueError("U must be square")
+
+    def Execute(self, reg) -> int:
+        self.ExecuteWithoutMeasurement(reg)
+        return reg.Measure(0, self.getFunctionStartQubit() - 1)
+
+    def ExecuteWithMultipleMeasurements(self, reg, nrMeasurements: int = 10000) -> dict:
+        self.ExecuteWithoutMeasurement(reg)
+        return reg.RepeatedMeasure(0, self.getFunctionStartQubit() - 1, nrMeasurements)
+
+    def getU(self) -> np.ndarray:
+        return self.U
+
+    def ExecuteWithoutMeasurement(self, reg) -> None:
+        self.Init(reg)
+        controlled = self.U.copy()
+        last = self.getFunctionStartQubit() - 1
+        for ctrl in range(last, 0, -1):
+            NQubitsControlledQuantumGate(self.getNrQubits(), controlled, self.getFunctionStartQubit(), ctrl).Execute(reg)
+            controlled = controlled @ controlled
+        NQubitsControlledQuantumGate(self.getNrQubits(), controlled, self.getFunctionStartQubit(), 0).Execute(reg)
+        self.IQFT(reg, False)
+
+
+class GroverOracle:
+    """Grover::Oracle (GroverAlgorithm.h:16-40): the identity with -1 at the marked state"""
+
+    def __init__(self):
+        self.correctQuestionState = 0
+
+    def setCorrectQuestionState(self, state: int) -> None:
+        self.correctQuestionState = state
+
+    def getOperatorMatrix(self, nrQubits: int) -> np.ndarray:
+        m = np.eye(1 << nrQubits, dtype=np.complex128)
+        if self.correctQuestionState < (1 << nrQubits):
+            m[self.correctQuestionState, self.correctQuestionState] = -1
+        return m
+
+
+class GroverAlgorithm(QuantumAlgorithm):
+    """Grover::GroverAlgorithm (GroverAlgorithm.h:42-124): round(pi / 4 sqrt(2^N)) rounds of the oracle and the
+    diffusion operator, both applied as ApplyOperatorMatrix of their (diagonal) matrices, which the
+    engine runs as one multiply per amplitude"""
+
+    def __init__(self, N: int = 3, addseed: int = 0, **kw):
+        super().__init__(N, addseed, **kw)
+        o00 = GroverOracle()
+        o00.setCorrectQuestionState(0)
+        self.OracleOp00 = o00.getOperatorMatrix(N)
+        self.hadamard = G.HadamardGate()
+        self.setCorrectQuestionState(0)
+
+    def setCorrectQuestionState(self, state: int) -> None:
+        o = GroverOracle()
+        o.setCorrectQuestionState(state)
+        self.OracleOp = o.getOperatorMatrix(self.getNrQubits())
+
+    def Execute(self) -> int:
+        self.ExecuteWithoutMeasurement()
+        return self.Measure()
+
+    def ExecuteWithMultipleMeasurements(self, nrMeasurements: int = 10000) -> dict:
+        self.ExecuteWithoutMeasurement()
+        return self.RepeatedMeasure(nrMeasurements)
+
+    def Init(self) -> None:
+        self.setToEqualSuperposition()
+
+    def ExecuteWithoutMeasurement(self) -> None:
+        self.Init()
+        repeat = int(math.floor(math.pi / 4.0 * math.sqrt(self.getNrBasisStates()) + 0.5))  # C round() for positives
+        for _ in range(repeat):
+            self.ApplyOperatorMatrix(self.OracleOp)
+            self.ApplyDiffusionOperator()
+
+    def ApplyHadamardOnAllQubits(self) -> None:
+        for i in range(self.getNrQubits()):
+            self.ApplyGate(self.hadamard, i)
+
+    def ApplyDiffusionOperator(self) -> None:
+        self.ApplyHadamardOnAllQubits()
+        self.ApplyOperatorMatrix(self.OracleOp00)
+        self.ApplyHadamardOnAllQubits()

@@ -247,11 +247,36 @@ namespace QC {
 				for (const auto& g : gates) computeGates.emplace_back(g);
 		}
 
+		// a diagonal matrix (every non-zero entry on the diagonal, as the Grover oracle and the Schrodinger
+		// operators are) runs as one multiply per amplitude (qcs_apply_diagonal)
 		void ApplyOperatorMatrix(const MatrixClass& m)
 		{
-			std::vector<double> rm(2 * static_cast<size_t>(m.rows()) * static_cast<size_t>(m.cols()));
-			detail::to_row_major(m, rm.data());
-			detail::qcs_check(qcs_apply_operator_matrix(handle, rm.data()), handle);
+			const size_t rows = static_cast<size_t>(m.rows()), cols = static_cast<size_t>(m.cols());
+			if (rows != NrBasisStates || cols != NrBasisStates) throw std::invalid_argument("The operator matrix does not match the register size");
+			bool diagonal = true;
+			for (size_t c = 0; c < cols && diagonal; ++c)
+				for (size_t r = 0; r < rows; ++r)
+					if (r != c && m(r, c) != std::complex<double>(0, 0))
+					{
+						diagonal = false;
+						break;
+					}
+			if (diagonal)
+			{
+				std::vector<double> d(2 * rows);
+				for (size_t i = 0; i < rows; ++i)
+				{
+					d[2 * i] = std::complex<double>(m(i, i)).real();
+					d[2 * i + 1] = std::complex<double>(m(i, i)).imag();
+				}
+				detail::qcs_check(qcs_apply_diagonal(handle, d.data()), handle);
+			}
+			else
+			{
+				std::vector<double> rm(2 * rows * cols);
+				detail::to_row_major(m, rm.data());
+				detail::qcs_check(qcs_apply_operator_matrix(handle, rm.data()), handle);
+			}
 			dirty = true;
 			if (recordGates)
 				computeGates.emplace_back(Gates::AppliedGate<MatrixClass>(m));

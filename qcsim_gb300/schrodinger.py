@@ -17,69 +17,13 @@ import math
 
 import numpy as np
 
-from .register import QubitRegister
+from .algorithms import QuantumAlgorithm
 
 
 def _polar(t: np.ndarray) -> np.ndarray:
     """cos t + i sin t, as std::polar(1, t); numpy's float64 cos and sin reduce arguments of any size
     exactly (the kinetic angles reach 1e12 and the walls 1e150)"""
     return np.ascontiguousarray(np.cos(t) + 1j * np.sin(t))
-
-
-class QuantumAlgorithm:
-    """QC::QuantumAlgorithm (QuantumAlgorithm.h:9-205): owns the register and forwards the state setters
-    and readers to it"""
-
-    def __init__(self, N: int = 3, addseed: int = 0, *, precision: str = "fp64", seed: int | None = None):
-        self.reg = QubitRegister(N, addseed, precision=precision, seed=seed)
-
-    def getNrQubits(self) -> int:
-        return self.reg.getNrQubits()
-
-    def getNrBasisStates(self) -> int:
-        return self.reg.getNrBasisStates()
-
-    def getBasisStateAmplitude(self, State: int) -> complex:
-        return self.reg.getBasisStateAmplitude(State)
-
-    def getBasisStateProbability(self, State: int) -> float:
-        return self.reg.getBasisStateProbability(State)
-
-    def setToBasisState(self, State: int) -> None:
-        self.reg.setToBasisState(State)
-
-    def setToQubitState(self, q: int) -> None:
-        self.reg.setToQubitState(q)
-
-    def setToCatState(self) -> None:
-        self.reg.setToCatState()
-
-    def setToEqualSuperposition(self) -> None:
-        self.reg.setToEqualSuperposition()
-
-    def setRawAmplitude(self, State: int, val: complex) -> None:
-        self.reg.setRawAmplitude(State, val)
-
-    def Clear(self) -> None:
-        self.reg.Clear()
-
-    def Normalize(self) -> None:
-        self.reg.Normalize()
-
-    def AdjustPhaseAndNormalize(self) -> None:
-        self.reg.AdjustPhaseAndNormalize()
-
-    def getRegister(self) -> QubitRegister:
-        return self.reg
-
-    def getRegisterStorage(self) -> np.ndarray:
-        return self.reg.getRegisterStorage()
-
-    def setRegisterStorage(self, vals) -> None:
-        self.reg.setRegisterStorage(vals)
-
-    def ApplyOperatorMatrix(self, m) -> None:
-        self.reg.ApplyOperatorMatrix(m)
 
 
 class SchrodingerSimulation(QuantumAlgorithm):

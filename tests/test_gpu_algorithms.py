@@ -1,0 +1,90 @@
+"""QCSim's algorithms over the engine, through the Python mirror of their classes: phase estimation
+(PhaseEstimation.h, with its controlled powers of U as NQubitsControlledQuantumGate on the device) and
+Grover's search with the diagonal oracle matrix (GroverAlgorithm.h).  The pre-measurement states are
+compared with a statevector computed by the oracle's contraction on the host (1e-12), and the measured
+answers with the checks of QCSim's own tests (PhaseEstimationTests.cpp:71-125: estimate within 0.05)."""
+import math
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def Q():
+    import qcsim_gb300
+    from qcsim_gb300 import _lib
+    try:
+        _lib.load()
+    except _lib.EngineUnavailable as e:
+        pytest.fail(f"engine not built: {e}")
+    return qcsim_gb300
+
+
+def host_hadamards(v, qubits):
+    from oracle import nqubits as O
+    h = np.array([[1, 1], [1, -1]], dtype=np.complex128) / math.sqrt(2)
+    for q in qubits:
+        v = O.apply_on_qubits(v, h, [q])
+    return v
+
+
+def host_phase_estimation(U, N, L):
+    """the circuit of PhaseEstimation::ExecuteWithoutMeasurement, before the IQFT"""
+    from oracle import nqubits as O
+    v = np.zeros(1 << N, dtype=np.complex128)
+    v[1 << L] = 1
+    v = host_hadamards(v, range(L))
+    cg = U.copy()
+    k = int(U.shape[0] - 1).bit_length()
+    for ctrl in range(L - 1, 0, -1):
+        v = O.apply_on_qubits(v, cg, list(range(L, L + k)), [ctrl])
+        cg = cg @ cg
+    return O.apply_on_qubits(v, cg, list(range(L, L + k)), [0])
+
+
+@pytest.mark.parametrize("phase", [1 / 4, 1 / 3, 1 / 2, 2 / 3, 3 / 4])
+def test_phase_estimation(Q, phase):
+    from qcsim_gb300 import algorithms as A, gates as G
+    U = G.PhaseShiftGate(phase * 2 * math.pi).getRawOperatorMatrix()
+    pe = A.PhaseEstimation(U, 4, 3)
+    reg = Q.QubitRegister(4, seed=7)
+    reg.setToQubitState(3)
+    counts = pe.ExecuteWithMultipleMeasurements(reg, 10000)
+    ranked = sorted(counts.items(), key=lambda kv: -kv[1])
+    mx, cnt = ranked[0]
+    assert abs(mx / 8 - phase) <= 0.05, (phase, ranked[:3])
+    second = ranked[1][0] if len(ranked) > 1 else -1
+    assert abs(pe.getPhase(mx, second, cnt / 10000) - phase) < 0.05
+    # the state before the measurements
+    reg2 = Q.QubitRegister(4, seed=7)
+    pe.ExecuteWithoutMeasurement(reg2)
+    want = host_phase_estimation(np.asarray(U), 4, 3)
+    from oracle import bind as B
+    ref = B.OracleRegister(4)
+    ref.set_state(want)
+    B.oracle().qo_qft(ref.h, 0, 2, 1, 0)
+    assert np.abs(reg2.getRegisterStorage() - ref.state()).max() < 1e-12
+    reg.close()
+    reg2.close()
+
+
+@pytest.mark.parametrize("n,marked", [(6, 45), (10, 613), (11, 1777)])
+def test_grover(Q, n, marked):
+    from qcsim_gb300 import algorithms as A
+    g = A.GroverAlgorithm(n, seed=3)
+    g.setCorrectQuestionState(marked)
+    g.ExecuteWithoutMeasurement()
+    got = g.getRegisterStorage()
+    v = np.full(1 << n, 1 / math.sqrt(1 << n), dtype=np.complex128)
+    for _ in range(int(math.floor(math.pi / 4 * math.sqrt(1 << n) + 0.5))):
+        v[marked] *= -1
+        v = host_hadamards(v, range(n))
+        v[0] *= -1
+        v = host_hadamards(v, range(n))
+    assert np.abs(got - v).max() < 1e-12
+    assert abs(got[marked]) ** 2 > 0.99
+    counts = g.RepeatedMeasure(1000)
+    assert max(counts, key=counts.get) == marked
+    g.close()
