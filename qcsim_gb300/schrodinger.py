@@ -14,6 +14,8 @@ from __future__ import annotations
 
 import ctypes as C
 import math
+import os
+from concurrent.futures import ThreadPoolExecutor
 
 import numpy as np
 
@@ -22,8 +24,23 @@ from .algorithms import QuantumAlgorithm
 
 def _polar(t: np.ndarray) -> np.ndarray:
     """cos t + i sin t, as std::polar(1, t); numpy's float64 cos and sin reduce arguments of any size
-    exactly (the kinetic angles reach 1e12 and the walls 1e150)"""
-    return np.ascontiguousarray(np.cos(t) + 1j * np.sin(t))
+    exactly (the kinetic angles reach 1e12 and the walls 1e150).  Large arrays are split over host
+    threads (numpy's ufuncs release the interpreter lock)."""
+    t = np.ascontiguousarray(t, dtype=np.float64)
+    out = np.empty(t.shape, dtype=np.complex128)
+    parts = out.view(np.float64).reshape(-1, 2)
+
+    def fill(lo: int, hi: int) -> None:
+        np.cos(t[lo:hi], out=parts[lo:hi, 0])
+        np.sin(t[lo:hi], out=parts[lo:hi, 1])
+
+    chunk = 1 << 20
+    if t.size <= chunk:
+        fill(0, t.size)
+    else:
+        with ThreadPoolExecutor(max_workers=min(32, os.cpu_count() or 1)) as ex:
+            list(ex.map(lambda lo: fill(lo, min(t.size, lo + chunk)), range(0, t.size, chunk)))
+    return out
 
 
 class SchrodingerSimulation(QuantumAlgorithm):
@@ -67,16 +84,16 @@ class SchrodingerSimulation(QuantumAlgorithm):
         """a square barrier (val > 0) or well in the middle, walls at both ends (Schrodinger.h:76-88)"""
         n = self.getNrBasisStates()
         half = n // 2
-        for i in range(max(1, half - halfwidth), min(n - 1, half + halfwidth)):
-            self.setPotential(i, val)
+        lo, hi = max(1, half - halfwidth), min(n - 1, half + halfwidth)
+        if lo < hi:
+            self.potential[lo:hi] = val
         self.setPotential(0, 1e150)
         self.setPotential(n - 1, 1e150)
 
     def setConstantPotentialToRight(self, val: float) -> None:
         """a step from the middle on, walls at both ends (Schrodinger.h:91-102)"""
         n = self.getNrBasisStates()
-        for i in range(n // 2, n):
-            self.setPotential(i, val)
+        self.potential[n // 2:] = val
         self.setPotential(0, 1e15)
         self.setPotential(n - 1, 1e150)
 
