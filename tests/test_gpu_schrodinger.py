@@ -52,7 +52,7 @@ def test_execute_matches_host_dft(Q, n, steps, precision):
     sim.reg.read_profile()
     sim.Execute()
     prof = sim.reg.read_profile()
-    assert set(prof) == {"tile_pass"}, prof
+    assert prof and all(k.startswith("tile_pass") for k in prof), prof
     got = sim.getRegisterStorage().astype(np.complex128)
     want = S.classical_fft_evolve(psi0, n, dt, dx, sim.potential, steps)
     tol = 1e-11 if precision == "fp64" else 1e-5
