@@ -1,7 +1,7 @@
 // Per-amplitude arithmetic of the gate kernels, shared by the per-gate kernels and the
 // shared-memory pass kernels so both produce identical results.
 //
-// GB300 executes FP64 FMAs at about 1/58 of its FP32 rate, so the FP64 amplitude updates are written
+// GB300 executes FP64 instructions at about 1/64 of its FP32 rate, so the FP64 amplitude updates are written
 // to use as few FP64 operations as the gate allows: permutations and sign/i flips use none, phases
 // touch only the half of the amplitudes they change, and rotations whose global scalar was factored
 // out on the host (the Unit* forms) cost one FMA per real component.
