@@ -3,8 +3,9 @@
 QuantumFourierTransform (QuantumFourierTransform.h:12-92), QubitsSwapper (QubitsSwapper.h:10-43),
 OneQubitGateTransform / HadamardTransform / XTransform (HadamardTransform.h:9-41), the dense operator
 gates NQubitsQuantumGate (NQubitsQuantumGate.h:9-78) / NQubitsControlledQuantumGate
-(NQubitsControlledQuantumGate.h:9-97), phase estimation (PhaseEstimation.h:11-231) and Grover's search
-with the diagonal oracle matrix (GroverAlgorithm.h:14-124).
+(NQubitsControlledQuantumGate.h:9-97), phase estimation (PhaseEstimation.h:11-231), Grover's search
+with the diagonal oracle matrix (GroverAlgorithm.h:14-124), Bernstein-Vazirani with its diagonal oracle
+(BernsteinVazirani.h:14-106) and the QFT adders DraperAdder / DraperAdderWithCarry (DraperAdder.h:11-117).
 
 The QFT runs as one engine call (qcs_qft), which applies the reference's gate sequence; the one-qubit
 transforms run as one gate list (qcs_one_qubit_transform); the dense operator gates run as one
@@ -426,3 +427,105 @@ class GroverAlgorithm(QuantumAlgorithm):
         self.ApplyHadamardOnAllQubits()
         self.ApplyOperatorMatrix(self.OracleOp00)
         self.ApplyHadamardOnAllQubits()
+
+
+class DraperAdder(QuantumAlgorithm):
+    """Adders::DraperAdder (DraperAdder.h:11-57): registers a (qubits 0 .. N-1) and b (N .. 2N-1); b <- a + b
+    mod 2^N by a QFT of b (no swaps), the controlled phases pi / 2^(q - N - c) from a's qubits c, and the
+    inverse QFT.  The phases commute, so they go to the engine as one gate list."""
+
+    def __init__(self, N: int = 3, addseed: int = 0, **kw):
+        super().__init__(2 * N, addseed, **kw)
+        self.n = N
+        self.fourier = QuantumFourierTransform(2 * N, N)
+        self.setToBasisState(0)
+
+    def Execute(self) -> int:
+        self.ExecuteWithoutMeasurement()
+        return self.Measure()
+
+    def ExecuteWithMultipleMeasurements(self, nrMeasurements: int = 10000) -> dict:
+        self.ExecuteWithoutMeasurement()
+        return self.RepeatedMeasure(nrMeasurements)
+
+    def _sum_phases(self) -> list:
+        ops = []
+        for qbit in range(self.n, 2 * self.n):
+            phase = math.pi
+            for cbit in range(qbit - self.n, -1, -1):
+                ops.append((G.ControlledPhaseShiftGate(phase), qbit, cbit))
+                phase *= 0.5
+        return ops
+
+    def ExecuteWithoutMeasurement(self) -> None:
+        self.fourier.QFT(self.reg, False)
+        self.ApplyGates(self._sum_phases())
+        self.fourier.IQFT(self.reg, False)
+
+
+class DraperAdderWithCarry(DraperAdder):
+    """Adders::DraperAdderWithCarry (DraperAdder.h:59-115): as DraperAdder with one more qubit (2N) above b
+    that receives the carry: the QFT covers b and the carry qubit, which gets the phases pi / 2^(N - c)
+    from a's qubits"""
+
+    def __init__(self, N: int = 3, addseed: int = 0, **kw):
+        QuantumAlgorithm.__init__(self, 2 * N + 1, addseed, **kw)
+        self.n = N
+        self.fourier = QuantumFourierTransform(2 * N + 1, N)
+        self.setToBasisState(0)
+
+    def ExecuteWithoutMeasurement(self) -> None:
+        self.fourier.QFT(self.reg, False)
+        ops = []
+        phase = math.pi / 2
+        for cbit in range(self.n - 1, -1, -1):
+            ops.append((G.ControlledPhaseShiftGate(phase), 2 * self.n, cbit))
+            phase *= 0.5
+        self.ApplyGates(ops + self._sum_phases())
+        self.fourier.IQFT(self.reg, False)
+
+
+class BernsteinVaziraniOracle:
+    """BernsteinVazirani::Oracle (BernsteinVazirani.h:16-57): -1 on the basis states whose bitwise product
+    with the hidden string has odd parity"""
+
+    def __init__(self):
+        self.stringFunction = 0
+
+    def setString(self, s: int) -> None:
+        self.stringFunction = s
+
+    def f(self, x: int) -> int:
+        return bin(x & self.stringFunction).count("1") % 2
+
+    def getOperatorMatrix(self, nrQubits: int) -> np.ndarray:
+        x = np.arange(1 << nrQubits)
+        parity = np.zeros(x.size, dtype=np.int64)
+        prod = x & self.stringFunction
+        while prod.any():
+            parity += prod & 1
+            prod >>= 1
+        return np.diag(np.where(parity % 2 == 1, -1.0, 1.0).astype(np.complex128))
+
+
+class BernsteinVaziraniAlgorithm(QuantumAlgorithm):
+    """BernsteinVazirani::BernsteinVaziraniAlgorithm (BernsteinVazirani.h:59-106): the equal superposition, the
+    oracle matrix (diagonal: one multiply per amplitude on the engine), Hadamards on every qubit, and a
+    measurement that returns the hidden string"""
+
+    def __init__(self, N: int = 3, addseed: int = 0, **kw):
+        super().__init__(N, addseed, **kw)
+        self.hadamard = G.HadamardGate()
+        self.setString(0)
+
+    def setString(self, s: int) -> None:
+        o = BernsteinVaziraniOracle()
+        o.setString(s)
+        self.OracleOp = o.getOperatorMatrix(self.getNrQubits())
+
+    def Execute(self) -> int:
+        self.setToEqualSuperposition()
+        self.ApplyOperatorMatrix(self.OracleOp)
+        for i in range(self.getNrQubits()):
+            self.ApplyGate(self.hadamard, i)
+        return self.Measure()

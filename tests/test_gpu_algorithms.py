@@ -88,3 +88,35 @@ def test_grover(Q, n, marked):
     counts = g.RepeatedMeasure(1000)
     assert max(counts, key=counts.get) == marked
     g.close()
+
+
+@pytest.mark.parametrize("carry", [False, True])
+def test_draper_adders(Q, carry):
+    """every pair of 3-bit inputs (AdderTests.cpp:270-340 draws random ones): the register ends in the basis
+    state a | (a + b) << 3, the sum mod 8 without the carry qubit, the full 4-bit sum with it"""
+    from qcsim_gb300 import algorithms as A
+    n = 3
+    adder = A.DraperAdderWithCarry(n, seed=5) if carry else A.DraperAdder(n, seed=5)
+    for a in range(8):
+        for b in range(8):
+            adder.setToBasisState(a | (b << n))
+            adder.ExecuteWithoutMeasurement()
+            s = a + b if carry else (a + b) % 8
+            want = a | (s << n)
+            state = adder.getRegisterStorage()
+            assert abs(abs(state[want]) - 1) < 1e-12, (a, b, carry)
+            assert adder.Measure() == want
+    adder.close()
+
+
+def test_bernstein_vazirani(Q):
+    """the measured value is the hidden string, with probability 1 (BernsteinVazirani.h:83-91)"""
+    from qcsim_gb300 import algorithms as A
+    rng = np.random.default_rng(17)
+    for n in (4, 9):
+        bv = A.BernsteinVaziraniAlgorithm(n, seed=2)
+        for s in [0, (1 << n) - 1] + [int(x) for x in rng.integers(0, 1 << n, 6)]:
+            bv.setString(s)
+            assert bv.Execute() == s
+            assert abs(bv.getBasisStateProbability(s) - 1) < 1e-12
+        bv.close()
