@@ -5,7 +5,8 @@ OneQubitGateTransform / HadamardTransform / XTransform (HadamardTransform.h:9-41
 gates NQubitsQuantumGate (NQubitsQuantumGate.h:9-78) / NQubitsControlledQuantumGate
 (NQubitsControlledQuantumGate.h:9-97), phase estimation (PhaseEstimation.h:11-231), Grover's search
 with the diagonal oracle matrix (GroverAlgorithm.h:14-124), Bernstein-Vazirani with its diagonal oracle
-(BernsteinVazirani.h:14-106) and the QFT adders DraperAdder / DraperAdderWithCarry (DraperAdder.h:11-117).
+(BernsteinVazirani.h:14-106), the QFT adders DraperAdder / DraperAdderWithCarry (DraperAdder.h:11-117) and the
+three-qubit flip and sign codes (ErrorCorrectionBase.h, ErrorCorrection3Qubits.h).
 
 The QFT runs as one engine call (qcs_qft), which applies the reference's gate sequence; the one-qubit
 transforms run as one gate list (qcs_one_qubit_transform); the dense operator gates run as one
@@ -529,3 +530,83 @@ class BernsteinVaziraniAlgorithm(QuantumAlgorithm):
         for i in range(self.getNrQubits()):
             self.ApplyGate(self.hadamard, i)
         return self.Measure()
+
+
+class ErrorCorrectionBase(QuantumAlgorithm):
+    """ErrorCorrection::ErrorCorrectionBase (ErrorCorrectionBase.h:8-50): a one-qubit state on qubit 0 and the
+    qubit an error hits (N or more: no error)"""
+
+    def __init__(self, N: int, addseed: int = 0, **kw):
+        super().__init__(N, addseed, **kw)
+        self.errorQubit = N
+        self.cnot, self.ccnot, self.x = G.CNOTGate(), G.ToffoliGate(), G.PauliXGate()
+        self.setToBasisState(0)
+
+    def SetState(self, alpha: complex, beta: complex) -> None:
+        self.Clear()
+        self.setRawAmplitude(0, alpha)
+        self.setRawAmplitude(1, beta)
+        self.Normalize()
+
+    def SetErrorQubit(self, q: int = 0) -> None:
+        self.errorQubit = q
+
+    def GetErrorQubit(self) -> int:
+        return self.errorQubit
+
+
+class ErrorCorrection3Qubits(ErrorCorrectionBase):
+    """ErrorCorrection3Qubits (ErrorCorrection3Qubits.h:8-33): repetition code on qubits 0-2"""
+
+    def __init__(self, addseed: int = 0, **kw):
+        super().__init__(3, addseed, **kw)
+
+    def Encode(self) -> None:
+        self.ApplyGate(self.cnot, 1, 0)
+        self.ApplyGate(self.cnot, 2, 0)
+
+    def DetectAndCorrect(self) -> None:
+        self.ApplyGate(self.cnot, 1, 0)
+        self.ApplyGate(self.cnot, 2, 0)
+        self.ApplyGate(self.ccnot, 0, 1, 2)
+
+
+class ErrorCorrection3QubitsFlip(ErrorCorrection3Qubits):
+    """bit-flip code (ErrorCorrection3Qubits.h:35-64): returns the syndrome on qubits 1-2 (3: qubit 0 was
+    flipped, 1 / 2: qubit 1 / 2, 0: none)"""
+
+    def Execute(self) -> int:
+        self.Encode()
+        self.ApplyError()
+        self.DetectAndCorrect()
+        return self.Measure(1, 2)
+
+    def ApplyError(self) -> None:
+        if self.errorQubit <= 2:
+            self.ApplyGate(self.x, self.errorQubit)
+
+
+class ErrorCorrection3QubitsSign(ErrorCorrection3Qubits):
+    """sign-flip code (ErrorCorrection3Qubits.h:67-110): the flip code in the Hadamard basis"""
+
+    def __init__(self, addseed: int = 0, **kw):
+        super().__init__(addseed, **kw)
+        self.hadamard = G.HadamardGate()
+
+    def Execute(self) -> int:
+        self.Encode()
+        self.ApplyHadamardOnAllQubits()
+        self.ApplyError()
+        self.ApplyHadamardOnAllQubits()
+        self.DetectAndCorrect()
+        return self.Measure(1, 2)
+
+    def ApplyError(self) -> None:
+        if self.errorQubit <= 2:
+            self.ApplyGate(self.hadamard, self.errorQubit)
+            self.ApplyGate(self.x, self.errorQubit)
+            self.ApplyGate(self.hadamard, self.errorQubit)
+
+    def ApplyHadamardOnAllQubits(self) -> None:
+        for i in range(self.getNrQubits()):
+            self.ApplyGate(self.hadamard, i)

@@ -120,3 +120,26 @@ def test_bernstein_vazirani(Q):
             assert bv.Execute() == s
             assert abs(bv.getBasisStateProbability(s) - 1) < 1e-12
         bv.close()
+
+
+@pytest.mark.parametrize("sign", [False, True])
+def test_three_qubit_codes(Q, sign):
+    """ErrorCorrectionTests.cpp:25-80 (flip) and its sign counterpart: for random states and every error
+    position, the syndrome names the flipped qubit and qubit 0 carries the original state (fidelity of
+    the collapsed register with alpha|m> + beta|m+1>, m = syndrome << 1)"""
+    from qcsim_gb300 import algorithms as A
+    rng = np.random.default_rng(23 + sign)
+    code = A.ErrorCorrection3QubitsSign(seed=4) if sign else A.ErrorCorrection3QubitsFlip(seed=4)
+    for _ in range(6):
+        a, b = complex(*rng.uniform(-1, 1, 2)), complex(*rng.uniform(-1, 1, 2))
+        nrm = math.sqrt(abs(a) ** 2 + abs(b) ** 2)
+        a, b = a / nrm, b / nrm
+        for q in range(4):
+            code.SetState(a, b)
+            code.SetErrorQubit(q)
+            res = code.Execute()
+            assert res == {0: 3, 1: 1, 2: 2, 3: 0}[q], (q, res)
+            want = np.zeros(8, dtype=np.complex128)
+            want[res << 1], want[(res << 1) | 1] = a, b
+            assert code.stateFidelity(want) > 1 - 1e-12
+    code.close()
