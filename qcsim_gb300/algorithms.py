@@ -6,7 +6,8 @@ gates NQubitsQuantumGate (NQubitsQuantumGate.h:9-78) / NQubitsControlledQuantumG
 (NQubitsControlledQuantumGate.h:9-97), phase estimation (PhaseEstimation.h:11-231), Grover's search
 with the diagonal oracle matrix (GroverAlgorithm.h:14-124), Bernstein-Vazirani with its diagonal oracle
 (BernsteinVazirani.h:14-106), the QFT adders DraperAdder / DraperAdderWithCarry (DraperAdder.h:11-117) and the
-three-qubit flip and sign codes (ErrorCorrectionBase.h, ErrorCorrection3Qubits.h).
+three-qubit flip and sign codes (ErrorCorrectionBase.h, ErrorCorrection3Qubits.h), and Shor's factoring with
+the tensor-product period finding (ShorAlgorithm.h:15-296, PhaseEstimation.h:100-149).
 
 The QFT runs as one engine call (qcs_qft), which applies the reference's gate sequence; the one-qubit
 transforms run as one gate list (qcs_one_qubit_transform); the dense operator gates run as one
@@ -610,3 +611,158 @@ class ErrorCorrection3QubitsSign(ErrorCorrection3Qubits):
     def ApplyHadamardOnAllQubits(self) -> None:
         for i in range(self.getNrQubits()):
             self.ApplyGate(self.hadamard, i)
+
+
+class FxBase:
+    """Shor::FxBase (ShorAlgorithm.h:15-52): x register = qubits 0 .. L-1, f register = L .. L+M-1, f(x) = A^x mod C"""
+
+    def __init__(self, L: int, M: int, C: int):
+        self.fRegisterStartQubit, self.fRegisterNrQubits, self.Number, self.A = L, M, C, 2
+
+    def setParam(self, a: int) -> None:
+        self.A = a
+
+    def getParam(self) -> int:
+        return self.A
+
+    def mod(self, v: int) -> int:
+        return v % self.Number
+
+    def getFunctionStartQubit(self) -> int:
+        return self.fRegisterStartQubit
+
+    def getFunctionNrQubits(self) -> int:
+        return self.fRegisterNrQubits
+
+
+class Fx(FxBase):
+    """Shor::Fx (ShorAlgorithm.h:54-104): for each x qubit l, the f register multiplied by A^(2^l) mod C where
+    that qubit is one (values f >= C unchanged).  The reference applies each as a 2^N x 2^N matrix; here
+    each is a 2^M x 2^M permutation controlled by qubit l on the device (ApplyOperatorOnQubits).  A^(2^l)
+    is formed as the reference forms it, by repeated squaring in 64-bit unsigned arithmetic."""
+
+    def Apply(self, reg) -> None:
+        L, M = self.fRegisterStartQubit, self.fRegisterNrQubits
+        d = 1 << M
+        an = self.A
+        for l in range(L):
+            perm = np.zeros((d, d), dtype=np.complex128)
+            mult = self.mod(an)
+            for f in range(d):
+                perm[self.mod(mult * f) if f < self.Number else f, f] = 1
+            reg.ApplyOperatorOnQubits(perm, list(range(L, L + M)), [l])
+            an = (an * an) & 0xFFFFFFFFFFFFFFFF
+
+
+class ShorPhaseEstimation(PhaseEstimationBase):
+    """SubAlgo::ShorPhaseEstimation (PhaseEstimation.h:100-149): Hadamards on x, f(x) into the f register, IQFT of
+    x (with swaps), then a measurement of the whole register"""
+
+    def __init__(self, f: FxBase, N: int = 7, L: int = 3):
+        super().__init__(N, L)
+        self.func = f
+
+    def Execute(self, reg) -> int:
+        self.ExecuteWithoutMeasurement(reg)
+        return reg.MeasureAll()
+
+    def ExecuteWithMultipleMeasurements(self, reg, nrMeasurements: int = 10000) -> dict:
+        self.ExecuteWithoutMeasurement(reg)
+        return reg.RepeatedMeasure(nrMeasurements)
+
+    def ExecuteWithoutMeasurement(self, reg) -> None:
+        self.Init(reg)
+        self.func.Apply(reg)
+        self.IQFT(reg)
+
+
+class ShorAlgorithm(QuantumAlgorithm):
+    """Shor::ShorAlgorithmBase + ShorAlgorithm (ShorAlgorithm.h:108-296): period finding on N qubits (x register
+    of L qubits) and the classical steps of factorize.  The reference draws the base a from a device-seeded
+    std::mt19937; here it comes from a seeded numpy generator (factor_seed)."""
+
+    def __init__(self, C: int = 15, N: int = 7, L: int = 3, addseed: int = 0, factor_seed: int | None = None, **kw):
+        super().__init__(N, addseed, **kw)
+        self.Number = C
+        self.fx = Fx(L, N - L, C)
+        self.phaseEstimation = ShorPhaseEstimation(self.fx, N, L)
+        self._rng = np.random.default_rng(factor_seed)
+
+    def setA(self, a: int) -> None:
+        self.fx.setParam(a)
+
+    def Execute(self) -> int:
+        return self.phaseEstimation.Execute(self.reg)
+
+    def ExecuteWithMultipleMeasurements(self, nrMeasurements: int = 10000) -> dict:
+        return self.phaseEstimation.ExecuteWithMultipleMeasurements(self.reg, nrMeasurements)
+
+    @staticmethod
+    def gcd(a: int, b: int) -> int:
+        while b:
+            a, b = b, a % b
+        return a
+
+    @staticmethod
+    def continuedFraction(val: float, limitIter: int, limitPrecision: float = 1e-5) -> list[int]:
+        res = []
+        intPart = int(val)
+        while limitIter:
+            limitIter -= 1
+            res.append(intPart)
+            val -= intPart
+            if abs(val) < limitPrecision:
+                break
+            val = 1.0 / val
+            intPart = int(val)
+        return res
+
+    @staticmethod
+    def getFractions(contFrac: list[int]) -> tuple[list[int], list[int]]:
+        nums, denoms = [], []
+        n2, n1, d2, d1 = 0, 1, 1, 0
+        for c in contFrac:
+            n, d = c * n1 + n2, c * d1 + d2
+            nums.append(n)
+            denoms.append(d)
+            n2, d2, n1, d1 = n1, d1, n, d
+        return nums, denoms
+
+    def factorize(self, numAttempts: int = 10) -> tuple[bool, int, int]:
+        """(quantum period finding used, p1, p2) as ShorAlgorithmBase::factorize (ShorAlgorithm.h:120-212)"""
+        C = self.Number
+        if C > 22:
+            return False, 0, 0
+        if C % 2 == 0:
+            return False, 2, C // 2
+        sq = int(round(math.sqrt(C)))
+        if sq * sq == C:
+            return False, sq, sq
+        L = self.fx.getFunctionStartQubit()
+        xmask = (1 << L) - 1
+        for _ in range(numAttempts):
+            a = int(self._rng.integers(2, C))  # uniform on [2, C - 1]
+            g = self.gcd(C, a)
+            if g > 1:
+                return False, g, C // g
+            self.setA(a)
+            state = self.Execute() & xmask
+            while not state:
+                state = self.Execute() & xmask
+            _, divs = self.getFractions(self.continuedFraction(state / (1 << L), L))
+            for p in divs[1:]:
+                if p % 2:
+                    p *= 2
+                while p < C:
+                    if self.fx.mod(a ** p) == 1:
+                        m = self.fx.mod(a ** (p // 2))
+                        if m != 1 and m != C - 1:
+                            p1, p2 = self.gcd(m - 1, C), self.gcd(m + 1, C)
+                            t1, t2 = C // p1, C // p2
+                            if p1 * t1 == C:
+                                p2 = t1
+                            else:
+                                p1 = t2
+                            return True, p1, p2
+                    p *= 2
+        return False, 1, C

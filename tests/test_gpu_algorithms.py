@@ -143,3 +143,57 @@ def test_three_qubit_codes(Q, sign):
             want[res << 1], want[(res << 1) | 1] = a, b
             assert code.stateFidelity(want) > 1 - 1e-12
     code.close()
+
+
+def host_shor_state(C, N, L, a):
+    """PhaseEstimation.h:129-145 on the host: f register = 1, Hadamards on x, the controlled multiplications
+    (the reference's 2^N x 2^N matrices, built here from their definition), then the oracle's IQFT"""
+    from oracle import bind as B
+    v = np.zeros(1 << N, dtype=np.complex128)
+    v[1 << L] = 1
+    v = host_hadamards(v, range(L))
+    an = a
+    for l in range(L):
+        out = np.zeros_like(v)
+        for k in range(1 << N):
+            x, f = k & ((1 << L) - 1), k >> L
+            if (x >> l) & 1 and f < C:
+                out[(((an % C) * f) % C) << L | x] += v[k]
+            else:
+                out[k] += v[k]
+        v = out
+        an = (an * an) & 0xFFFFFFFFFFFFFFFF
+    ref = B.OracleRegister(N)
+    ref.set_state(v)
+    B.oracle().qo_qft(ref.h, 0, L - 1, 1, 1)
+    return ref.state()
+
+
+@pytest.mark.parametrize("C,N,L,a", [(15, 7, 3, 7), (15, 7, 3, 2), (21, 9, 4, 5)])
+def test_shor_period_finding(Q, C, N, L, a):
+    """the pre-measurement state against the host; measured x values are multiples of 2^L / r (r = the order of
+    a mod C, when r divides 2^L)"""
+    from qcsim_gb300 import algorithms as A
+    shor = A.ShorAlgorithm(C, N, L, seed=11)
+    shor.setA(a)
+    shor.phaseEstimation.ExecuteWithoutMeasurement(shor.reg)
+    assert np.abs(shor.getRegisterStorage() - host_shor_state(C, N, L, a)).max() < 1e-12
+    r = next(k for k in range(1, C) if pow(a, k, C) == 1)
+    if (1 << L) % r == 0:
+        counts = shor.reg.RepeatedMeasure(2000)
+        xs = {s & ((1 << L) - 1) for s in counts}
+        assert xs <= {m * ((1 << L) // r) for m in range(r)}, (xs, r)
+    shor.close()
+
+
+def test_shor_factorizes_15(Q):
+    """Tests.cpp:76-88: 15 = 5 x 3"""
+    from qcsim_gb300 import algorithms as A
+    found = False
+    for seed in range(5):
+        shor = A.ShorAlgorithm(15, 7, 3, seed=seed, factor_seed=seed)
+        used, p1, p2 = shor.factorize()
+        shor.close()
+        assert sorted((p1, p2)) == [3, 5], (used, p1, p2)
+        found = found or used
+    assert found
