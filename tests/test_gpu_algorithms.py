@@ -197,3 +197,29 @@ def test_shor_factorizes_15(Q):
         assert sorted((p1, p2)) == [3, 5], (used, p1, p2)
         found = found or used
     assert found
+
+
+def test_vqe_energy_estimate_and_search(Q):
+    """VQETests.cpp:9-65: H = 3X - 2Y + Z on one qubit (ground energy -sqrt(14)); the sampled energy of a point
+    agrees with the exact expectation of the same circuit, and the Nelder-Mead search ends below -3"""
+    from qcsim_gb300 import vqe as V
+    rng = np.random.default_rng(31)
+    solver = V.VariationalQuantumEigensolver(1, seed=9)
+    for op, c in (("X", 3.0), ("Y", -2.0), ("Z", 1.0)):
+        t = V.PauliStringVQE(1)
+        t.setOperatorForQubit(0, op)
+        t.setCoefficient(c)
+        solver.AddTerm(t)
+    th, ph = 1.1, 2.3
+    # exact <H> of RZ(ph) RY(th)|0>: Bloch vector (sin th cos ph, sin th sin ph, cos th)
+    exact = 3 * math.sin(th) * math.cos(ph) - 2 * math.sin(th) * math.sin(ph) + math.cos(th)
+    est = solver.EstimateEnergy([th, ph], 40000)
+    assert abs(est - exact) < 0.1, (est, exact)
+    theta, phi, radius = rng.uniform() * math.pi / 2, rng.uniform() * math.pi, 0.35
+    R = rng.uniform() * 2 * math.pi / 3
+    solver.SetVertices([[theta + radius * math.cos(R + v * 2 * math.pi / 3), phi + radius * math.sin(R + v * 2 * math.pi / 3)]
+                        for v in range(3)])
+    solver.Execute()
+    assert solver.GetMinEnergy() < -3.0, solver.GetMinEnergy()
+    assert len(solver.GetMinVertex()) == 2
+    solver.close()
