@@ -53,10 +53,45 @@ template <typename T>
 __global__ void __launch_bounds__(kRedThreads) k_masked_prob(const cplx_t<T>* __restrict__ s, uint64_t N, uint64_t mask, uint64_t value, double* part) {
 	__shared__ double sh[kRedThreads];
 	const uint64_t stride = static_cast<uint64_t>(gridDim.x) * blockDim.x;
-	double acc = 0;
-	for (uint64_t i = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < N; i += stride)
-		if ((i & mask) == value) acc = __dadd_rn(acc, probd<T>(s[i]));
-	const double r = block_sum(acc, sh);
+	const uint64_t t0 = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+	// four independent loads and sums in flight per thread (one dependent sum chain per thread leaves the
+	// memory system idle); the four sums are folded in a fixed order, so the result is repeatable.  |a|^2
+	// accumulates by two FMAs (the FP64 pipe bounds this kernel on GB300); these sums serve
+	// GetQubitProbability, Normalize and the collapse factor, whose results the reference's own
+	// summation order already leaves equal only to rounding -- the sampling scans keep probd.
+	double acc[4] = {0, 0, 0, 0};
+	auto add = [](double a, const cplx_t<T>& v) {
+		const double x = static_cast<double>(v.x), y = static_cast<double>(v.y);
+		return fma(y, y, fma(x, x, a));
+	};
+	if (mask && !(mask & (mask - 1)) && mask < N && (value & ~mask) == 0) {
+		// one qubit of the register (GetQubitProbability): enumerate only the amplitudes with that bit at
+		// `value` (j < N/2 with the bit inserted stays below N; a bit above the register takes the general
+		// loop, which finds no amplitude)
+		const uint64_t M = N >> 1, low = mask - 1;
+		auto at = [&](uint64_t j) { return s[((j & ~low) << 1) | (j & low) | value]; };
+		uint64_t j = t0;
+		for (; j + 3 * stride < M; j += 4 * stride) {
+			const cplx_t<T> a0 = at(j), a1 = at(j + stride), a2 = at(j + 2 * stride), a3 = at(j + 3 * stride);
+			acc[0] = add(acc[0], a0);
+			acc[1] = add(acc[1], a1);
+			acc[2] = add(acc[2], a2);
+			acc[3] = add(acc[3], a3);
+		}
+		for (; j < M; j += stride) acc[0] = add(acc[0], at(j));
+	} else {
+		uint64_t i = t0;
+		for (; i + 3 * stride < N; i += 4 * stride) {
+#pragma unroll
+			for (int u = 0; u < 4; ++u) {
+				const uint64_t k = i + u * stride;
+				if ((k & mask) == value) acc[u] = add(acc[u], s[k]);
+			}
+		}
+		for (; i < N; i += stride)
+			if ((i & mask) == value) acc[0] = add(acc[0], s[i]);
+	}
+	const double r = block_sum(__dadd_rn(__dadd_rn(acc[0], acc[1]), __dadd_rn(acc[2], acc[3])), sh);
 	if (threadIdx.x == 0) part[blockIdx.x] = r;
 }
 
