@@ -22,12 +22,12 @@ __global__ void __launch_bounds__(kThreads) k_compare(const A* __restrict__ a, c
 		const double sx = a[i].x, sy = a[i].y, tx = b[i].x, ty = b[i].y;
 		const double ax = sa.x * sx - sa.y * sy, ay = sa.x * sy + sa.y * sx;
 		const double bx = sb.x * tx - sb.y * ty, by = sb.x * ty + sb.y * tx;
-		re += ax * bx + ay * by;
-		im += ax * by - ay * bx;
-		na += ax * ax + ay * ay;
-		nb += bx * bx + by * by;
+		re = fma(ay, by, fma(ax, bx, re));
+		im = fma(-ay, bx, fma(ax, by, im));
+		na = fma(ay, ay, fma(ax, ax, na));
+		nb = fma(by, by, fma(bx, bx, nb));
 		const double dx = ax - bx, dy = ay - by;
-		mx = fmax(mx, sqrt(dx * dx + dy * dy));
+		mx = fmax(mx, fma(dy, dy, dx * dx));  // squared; one square root at the end (FP64 pipe)
 	}
 	sh[0][threadIdx.x] = re;
 	sh[1][threadIdx.x] = im;
@@ -96,6 +96,6 @@ extern "C" int qcs_compare(qcs_handle h, qcs_handle other, double* fidelity_out,
 	}
 	const double den = r[2] * r[3];
 	*fidelity_out = den > 0 ? (r[0] * r[0] + r[1] * r[1]) / den : 0.0;
-	*max_abs_diff_out = r[4];
+	*max_abs_diff_out = std::sqrt(r[4]);
 	return QCS_OK;
 }
