@@ -551,3 +551,26 @@ def test_fp32_long_factored_sequences(Q, batched):
     assert np.all(np.isfinite(got.view(np.float32)))
     assert np.abs(got - v).max() < 1e-5
     reg.close()
+
+
+@pytest.mark.parametrize("n,precision", [(34, "fp64"), (35, "fp32")])
+def test_largest_registers(Q, n, precision):
+    """the largest register of each precision that HBM holds (2^n amplitudes = 256 GiB): gates through the
+    pass planner (tiles with 22-23 fixed qubits), then exact qubit probabilities"""
+    import torch
+    from qcsim_gb300 import gates as G
+    free, _ = torch.cuda.mem_get_info()
+    need = (1 << n) * (16 if precision == "fp64" else 8)
+    if free < need + (4 << 30):
+        pytest.skip(f"{free / 2**30:.0f} GiB free, {need / 2**30:.0f} GiB needed")
+    reg = Q.QubitRegister(n, seed=1, precision=precision)
+    top = n - 1
+    reg.ApplyGates([(G.HadamardGate(), top), (G.HadamardGate(), 0), (G.CNOTGate(), 17, top), (G.PauliXGate(), 9)])
+    tol = 1e-12 if precision == "fp64" else 1e-6
+    assert abs(reg.GetQubitProbability(top) - 0.5) < tol
+    assert abs(reg.GetQubitProbability(17) - 0.5) < tol
+    assert abs(reg.GetQubitProbability(0) - 0.5) < tol
+    assert abs(reg.GetQubitProbability(9) - 1.0) < tol
+    assert reg.GetQubitProbability(5) < tol
+    assert abs(reg.getBasisStateAmplitude((1 << top) | (1 << 17) | (1 << 9)) - 0.5) < tol
+    reg.close()
