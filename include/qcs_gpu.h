@@ -193,10 +193,12 @@ uint64_t qcs_qaoa_batch_amplitudes(qcs_qaoa_batch_handle b);
 const char* qcs_qaoa_batch_last_error(qcs_qaoa_batch_handle b);
 int qcs_qaoa_batch_destroy(qcs_qaoa_batch_handle b);
 
-/* ---- dense operators on a few qubits (the kernel of the fused path; NQubitsQuantumGate-style
- * operators, NQubitsQuantumGate.h:27-47, without building the 2^n x 2^n matrix) ----
+/* ---- one fused block (no reference counterpart): a dense 2^k x 2^k operator applied as one operation of a
+ * shared-memory pass, the form the fused path gives its blocks (the learned cost model times blocks
+ * through it) ----
  * m: 2^k x 2^k complex, row-major interleaved; matrix bit j is qubits[j] (any order, distinct);
- * k <= 5 (FP32 registers) or 4 (FP64 registers) */
+ * k <= 5 (FP32 registers) or 4 (FP64 registers).  General dense operators (up to 10 qubits, with
+ * controls) go through qcs_apply_operator_on_qubits. */
 int qcs_apply_matrix(qcs_handle h, const uint32_t* qubits, uint32_t k, const double* m);
 
 /* ---- learned cost model (no reference counterpart): a 3-layer MLP, F inputs -> 64 -> 64 -> 1 with
