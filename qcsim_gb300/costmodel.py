@@ -260,7 +260,7 @@ def attach(reg, mlp: Mlp, pass_ms: np.ndarray) -> None:
     t = np.ascontiguousarray(pass_ms, dtype=np.float64)
     reg._cost_model = (mlp, t)  # keep alive with the register
     reg._ck(lib.qcs_set_cost_model(reg.handle, mlp.handle, L.dptr(t), len(t)))
-    reg.set_fusion(2)
+    reg.set_fusion(2, 5)  # candidate partitions with blocks of up to 5 qubits
 
 
 def train_from_timings(X: np.ndarray, T: np.ndarray, steps: int = 3000, lr: float = 3e-3, seed: int = 1,

@@ -93,7 +93,7 @@ struct qcs_register {
 	void* batch = nullptr;                 // planner buffers (batch.cu)
 	int batch_mode = 1;                    // QCS_OPT_PASSES
 	int fusion = -1;                       // QCS_OPT_FUSION (-1: by precision)
-	int fusion_max = 5;                    // QCS_OPT_FUSION_MAX_QUBITS
+	int fusion_max = 3;                    // QCS_OPT_FUSION_MAX_QUBITS
 	int tensor_cores = 1;                  // QCS_OPT_TENSOR_CORES
 	void* cost_ctx = nullptr;              // learned partition choice (costmodel.cu)
 	double last_predicted_ms = 0;          // its prediction for the last fused gate list
