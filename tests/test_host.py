@@ -111,10 +111,13 @@ REF_QCSIM = Path("/root/reference/QCSim")
 
 
 @pytest.mark.skipif(not REF_QCSIM.exists(), reason="needs the QCSim sources")
-def test_cpp_dropin_compiles_against_reference_headers():
-    """QCSim's own algorithm headers (QFT, Grover, Draper adder, QAOA, phase estimation), unmodified,
-    compile and link against the GPU-backed QubitRegister.h of qcsim_gb300/cpp.  The reference's
-    quoted includes are resolved through the include path (-I-), so the drop-in headers win."""
+@pytest.mark.parametrize("program", ["dropin_check", "dropin_algorithms"])
+def test_cpp_dropin_compiles_against_reference_headers(program):
+    """QCSim's own algorithm headers, unmodified, compile and link against the GPU-backed QubitRegister.h
+    of qcsim_gb300/cpp: QFT, Grover, Draper adder, QAOA and phase estimation (dropin_check.cpp); Shor,
+    VQE, error correction, Bernstein-Vazirani, Deutsch-Jozsa, Simon, superdense coding, teleportation,
+    quantum counting, the adders, q-means, CHSH and BB84 (dropin_algorithms.cpp).  The reference's quoted
+    includes are resolved through the include path (-I-), so the drop-in headers win."""
     import glob
     import shutil
     import subprocess
@@ -128,11 +131,11 @@ def test_cpp_dropin_compiles_against_reference_headers():
     out.mkdir(exist_ok=True)
     cmd = [gxx, "-std=c++17", "-O1", f"-I{ROOT / 'qcsim_gb300' / 'cpp'}", f"-I{ROOT / 'include'}", f"-I{REF_QCSIM}", "-I-",
            f"-I{ROOT / 'oracle' / 'eigen_shim'}"] + [f"-I{p}" for p in pstl[-1:]] + [
-           str(ROOT / "tests" / "cpp" / "dropin_check.cpp"), "-o", str(out / "dropin_check"),
+           str(ROOT / "tests" / "cpp" / f"{program}.cpp"), "-o", str(out / program),
            f"-L{L.LIB_PATH.parent}", "-lqcs_gpu", f"-Wl,-rpath,{L.LIB_PATH.parent}"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     assert r.returncode == 0, r.stderr[-3000:]
-    assert (out / "dropin_check").exists()
+    assert (out / program).exists()
 
 
 def test_fusion_plan_covers_every_gate():
