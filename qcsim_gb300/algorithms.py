@@ -5,7 +5,8 @@ OneQubitGateTransform / HadamardTransform / XTransform (HadamardTransform.h:9-41
 gates NQubitsQuantumGate (NQubitsQuantumGate.h:9-78) / NQubitsControlledQuantumGate
 (NQubitsControlledQuantumGate.h:9-97), phase estimation (PhaseEstimation.h:11-231), Grover's search
 with the diagonal oracle matrix (GroverAlgorithm.h:14-124), Bernstein-Vazirani with its diagonal oracle
-(BernsteinVazirani.h:14-106), the QFT adders DraperAdder / DraperAdderWithCarry (DraperAdder.h:11-117) and the
+(BernsteinVazirani.h:14-106), Deutsch-Jozsa (DeutschJozsa.h:16-137) and Simon's algorithm (SimonAlgorithm.h:15-248)
+with their permutation oracles, the QFT adders DraperAdder / DraperAdderWithCarry (DraperAdder.h:11-117) and the
 three-qubit flip and sign codes (ErrorCorrectionBase.h, ErrorCorrection3Qubits.h), and Shor's factoring with
 the tensor-product period finding (ShorAlgorithm.h:15-296, PhaseEstimation.h:100-149).
 
@@ -16,6 +17,7 @@ qcs_apply_operator_on_qubits call on their 2^k x 2^k operator.
 from __future__ import annotations
 
 import ctypes as C
+import enum
 import math
 
 import numpy as np
@@ -531,6 +533,166 @@ class BernsteinVaziraniAlgorithm(QuantumAlgorithm):
         for i in range(self.getNrQubits()):
             self.ApplyGate(self.hadamard, i)
         return self.Measure()
+
+
+class DeutschJozsaAlgorithm(QuantumAlgorithm):
+    """DeutschJozsa::DeutschJozsaAlgorithm (DeutschJozsa.h:16-137): is f on N - 1 bits constant or balanced?
+    The register starts in |1>|0...0> (the answer qubit is the top one), gets Hadamards on every qubit, the
+    oracle U|y>|x> = |y + f(x)>|x> as a 2^N x 2^N permutation matrix (ApplyOperatorMatrix), and Hadamards on
+    every qubit but the top one; the x part of the measured state is zero exactly for a constant f.  The
+    reference shuffles the balanced function with a clock-seeded generator; here it is a seeded numpy one
+    (function_seed)."""
+
+    class FunctionType(enum.IntEnum):
+        constantZero = 0
+        constantOne = 1
+        balanced = 2
+
+    def __init__(self, N: int = 2, addseed: int = 0, function_seed: int | None = None, **kw):
+        assert N >= 2
+        super().__init__(N, addseed, **kw)
+        self.hadamard = G.HadamardGate()
+        self.functionType = self.FunctionType.constantZero
+        self.fvalues = np.zeros(0, dtype=np.int64)
+        self._rng = np.random.default_rng(function_seed)
+
+    def Execute(self) -> int:
+        self.setToQubitState(self.getNrQubits() - 1)
+        n = self.getNrQubits()
+        self.ApplyGates([(self.hadamard, q) for q in range(n)])
+        self.ApplyOperatorMatrix(self.getOracleMatrix())
+        self.ApplyGates([(self.hadamard, q) for q in range(n - 1)])
+        return self.Measure()
+
+    def WasConstantResult(self, state: int) -> bool:
+        return (state & ((self.getNrBasisStates() - 1) >> 1)) == 0
+
+    def setFunction(self, ft) -> None:
+        """balanced: half of the 2^(N-1) inputs map to 1, in a random order (DeutschJozsa.h:54-72)"""
+        self.functionType = self.FunctionType(ft)
+        if self.functionType == self.FunctionType.balanced:
+            size = self.getNrBasisStates() >> 1
+            v = np.zeros(size, dtype=np.int64)
+            v[: size >> 1] = 1
+            self.fvalues = self._rng.permutation(v)
+        else:
+            self.fvalues = np.zeros(0, dtype=np.int64)
+
+    def getFunction(self):
+        return self.functionType
+
+    def f(self, x):
+        if self.functionType == self.FunctionType.balanced:
+            return self.fvalues[x]
+        return np.full(np.shape(x), int(self.functionType), dtype=np.int64)
+
+    def getOracleMatrix(self) -> np.ndarray:
+        """U(ket, bra) = 1 where x_ket = x_bra and y_ket = y_bra + f(x_bra) mod 2 (DeutschJozsa.h:104-129)"""
+        nb = self.getNrBasisStates()
+        top = self.getNrQubits() - 1
+        bra = np.arange(nb)
+        x = bra & ((nb - 1) >> 1)
+        ket = x | ((self.f(x) ^ (bra >> top)) << top)
+        u = np.zeros((nb, nb), dtype=np.complex128)
+        u[ket, bra] = 1
+        return u
+
+
+class SimonFunction:
+    """Simon::SimonFunction (SimonAlgorithm.h:15-97): a random function on N bits that is one-to-one for the
+    string 0 and two-to-one with f(x) = f(x ^ s) otherwise.  The reference shuffles with a clock-seeded
+    generator; here it is a seeded numpy one."""
+
+    def __init__(self, rng=None):
+        self.stringFunction = 0
+        self.functionTable = np.zeros(0, dtype=np.int64)
+        self._rng = rng if rng is not None else np.random.default_rng()
+
+    def __call__(self, x):
+        if self.functionTable.size == 0:
+            return np.zeros(np.shape(x), dtype=np.int64)
+        return self.functionTable[np.asarray(x) & (self.functionTable.size - 1)]
+
+    def setString(self, s: int, N: int) -> None:
+        """a shuffled identity table, then for every x its partner x ^ s (taken once, in a shuffled order)
+        gets the same value (SimonAlgorithm.h:27-64)"""
+        self.stringFunction = s
+        nb = 1 << N
+        table = self._rng.permutation(nb)
+        indices = list(self._rng.permutation(nb))
+        for x in range(nb):
+            for i in range(nb):
+                y = indices[i]
+                if y is None or x == y:
+                    continue
+                if (x ^ y) == s:
+                    table[x] = table[y]
+                    indices[i] = None
+                    break
+        self.functionTable = table.astype(np.int64)
+
+    def checkFunction(self) -> bool:
+        """one-to-one for s = 0; otherwise every value taken by exactly a pair {a, a ^ s} (SimonAlgorithm.h:66-93)"""
+        t = self.functionTable
+        if self.stringFunction == 0:
+            return len(set(t.tolist())) == t.size
+        groups: dict[int, list[int]] = {}
+        for i, v in enumerate(t.tolist()):
+            groups.setdefault(v, []).append(i)
+        if len(groups) != t.size // 2:
+            return False
+        return all(len(g) == 2 and (g[0] ^ g[1]) in (0, self.stringFunction) for g in groups.values())
+
+
+class SimonAlgorithm(QuantumAlgorithm):
+    """Simon::SimonAlgorithm (SimonAlgorithm.h:148-248): 2N qubits, x in the low N and f(x) in the high N.  Each
+    round prepares |0>, Hadamards on the x half, the oracle B|x>|y> = |x>|y ^ f(x)> as a permutation matrix
+    (ApplyOperatorMatrix), Hadamards on the x half again and a measurement of the x half; every outcome b has
+    b.s = 0 mod 2.  After up to 300 rounds (or all 2^N outcomes, meaning s = 0) the candidates of s with odd
+    parity against a measured b are removed; Execute returns the one left, 0, or 2^N when ambiguous."""
+
+    def __init__(self, N: int = 3, addseed: int = 0, function_seed: int | None = None, **kw):
+        assert N >= 2
+        super().__init__(2 * N, addseed, **kw)
+        self.hadamard = G.HadamardGate()
+        self.f = SimonFunction(np.random.default_rng(function_seed))
+        self.setString(0)
+
+    def setString(self, s: int) -> None:
+        N = self.getNrQubits() >> 1
+        self.f.setString(s, N)
+        self.OracleOp = self.getOracleMatrix()
+
+    def getOracleMatrix(self) -> np.ndarray:
+        """B(ket, bra) = 1 where x_ket = x_bra and y_ket = y_bra ^ f(x_bra) (SimonAlgorithm.h:104-136)"""
+        N = self.getNrQubits() >> 1
+        nb = self.getNrBasisStates()
+        bra = np.arange(nb)
+        xmask = (1 << N) - 1
+        x = bra & xmask
+        ket = x | ((bra & (xmask << N)) ^ (self.f(x) << N))
+        u = np.zeros((nb, nb), dtype=np.complex128)
+        u[ket, bra] = 1
+        return u
+
+    def Execute(self) -> int:
+        N = self.getNrQubits() >> 1
+        mask = (1 << N) - 1
+        measurements: dict[int, int] = {}
+        for _ in range(300):
+            self.setToBasisState(0)
+            self.ApplyGates([(self.hadamard, q) for q in range(N)])
+            self.ApplyOperatorMatrix(self.OracleOp)
+            self.ApplyGates([(self.hadamard, q) for q in range(N)])
+            m = self.Measure(0, N - 1)
+            measurements[m] = measurements.get(m, 0) + 1
+            if len(measurements) == 1 << N:
+                return 0
+        candidates = set(range(1, mask + 1))
+        for b in measurements:
+            if b:
+                candidates = {c for c in candidates if bin(c & b).count("1") % 2 == 0}
+        return next(iter(candidates)) if len(candidates) == 1 else mask + 1
 
 
 class ErrorCorrectionBase(QuantumAlgorithm):

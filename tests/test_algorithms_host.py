@@ -53,3 +53,109 @@ def test_oracles():
     g.setCorrectQuestionState(5)
     gm = g.getOperatorMatrix(3)
     assert gm[5, 5] == -1 and np.trace(gm) == 6
+
+
+class _HostRegister:
+    """stands in for the engine register where only the register's size is read"""
+
+    def __init__(self, N, *a, **kw):
+        self.N = N
+
+    def getNrQubits(self):
+        return self.N
+
+    def getNrBasisStates(self):
+        return 1 << self.N
+
+
+def _host_algorithm(monkeypatch, cls, *args, **kw):
+    def init(self, N=3, addseed=0, **_):
+        self.reg = _HostRegister(N)
+    monkeypatch.setattr(A.QuantumAlgorithm, "__init__", init)
+    return cls(*args, **kw)
+
+
+def _is_permutation(u):
+    return (np.count_nonzero(u) == u.shape[0] and np.all(np.abs(u).sum(axis=0) == 1)
+            and np.all(np.abs(u).sum(axis=1) == 1))
+
+
+def test_simon_function_and_oracle(monkeypatch):
+    """SimonFunction (SimonAlgorithm.h:15-97) is one-to-one for s = 0 and two-to-one with f(x) = f(x ^ s)
+    otherwise; the oracle (SimonAlgorithm.h:104-136) maps |x>|y> to |x>|y ^ f(x)>"""
+    for N in (2, 3, 4):
+        for s in range(1 << N):
+            f = A.SimonFunction(np.random.default_rng(s))
+            f.setString(s, N)
+            assert f.checkFunction()
+            if s:
+                assert all(f(x) == f(x ^ s) for x in range(1 << N))
+    simon = _host_algorithm(monkeypatch, A.SimonAlgorithm, 3, function_seed=4)
+    simon.setString(0b101)
+    u = simon.OracleOp
+    assert _is_permutation(u)
+    for bra in range(64):
+        x, y = bra & 7, bra >> 3
+        assert u[x | ((y ^ int(simon.f(x))) << 3), bra] == 1
+
+
+def test_deutsch_jozsa_oracle(monkeypatch):
+    """DeutschJozsa.h:54-72, :104-129: balanced functions take the value 1 on half the inputs; the oracle maps
+    |y>|x> to |y + f(x)>|x> with y the top qubit"""
+    dj = _host_algorithm(monkeypatch, A.DeutschJozsaAlgorithm, 5, function_seed=2)
+    FT = A.DeutschJozsaAlgorithm.FunctionType
+    for ft, ones in ((FT.constantZero, 0), (FT.constantOne, 16), (FT.balanced, 8)):
+        dj.setFunction(ft)
+        fx = dj.f(np.arange(16))
+        assert int(fx.sum()) == ones
+        u = dj.getOracleMatrix()
+        assert _is_permutation(u)
+        for bra in range(32):
+            assert u[(bra & 15) | (((bra >> 4) ^ int(fx[bra & 15])) << 4), bra] == 1
+    assert dj.WasConstantResult(16) and not dj.WasConstantResult(3)
+
+
+def test_n_controlled_not_with_ancilla():
+    """NControlledNotWithAncilla.h:27-100: the target flips exactly when every control is set, and the
+    ancillas are returned to 0 (the recorded ancilla computation is undone)"""
+    from qcsim_gb300 import counting as Q
+    for nc in range(1, 8):
+        controls = list(range(nc))
+        target, anc0 = nc, nc + 1
+        g = Q.NControlledNotWithAncilla()
+        g.SetControlQubits(controls)
+        g.SetTargetQubit(target)
+        g.SetStartAncillaQubits(anc0)
+        seq = Q.GateSequence()
+        g.Execute(seq)
+        for c in range(1 << nc):
+            bits = c
+            for gate, t, c1, c2 in seq.ops:
+                if gate.getQubitsNumber() == 3:
+                    if (bits >> c1) & (bits >> c2) & 1:
+                        bits ^= 1 << t
+                elif (bits >> c1) & 1:
+                    bits ^= 1 << t
+            assert bits >> anc0 == 0, (nc, c)
+            assert (bits >> target) & 1 == (c == (1 << nc) - 1), (nc, c)
+
+
+def test_quantum_counting_circuit_on_the_oracle(monkeypatch):
+    """QuantumCountingAlgorithm.h:104-179 and CountingTests (Tests.cpp:619-663) at 3 Grover qubits and 6
+    precision qubits: the gate list plus the inverse QFT (no swaps) on the CPU oracle; the most probable
+    precision value gives the number of marked states, and the ancillas end in |0>"""
+    from oracle import bind as B
+    from qcsim_gb300 import counting as Q
+    P, Gq = 6, 3
+    n = P + 2 * Gq
+    rng = np.random.default_rng(11)
+    for marked in range(0, (1 << Gq) + 1):
+        qc = _host_algorithm(monkeypatch, Q.QuantumCountingAlgorithm, P, Gq)
+        qc.SetMarkedStates(rng.permutation(1 << Gq)[:marked].tolist())
+        ref = B.OracleRegister(n)
+        ref.apply(qc.circuit())
+        assert B.oracle().qo_qft(ref.h, 0, P - 1, 1, 0) == 0
+        p = np.abs(ref.state()) ** 2
+        assert p[np.arange(p.size) >> (P + Gq) != 0].sum() < 1e-20
+        px = np.bincount(np.arange(p.size) & ((1 << P) - 1), weights=p)
+        assert qc.GetCountForState(int(np.argmax(px))) == marked

@@ -1,0 +1,154 @@
+"""QCSim's oracle algorithms, teleportation family and quantum counting over the engine, through the Python
+mirror of their classes, with the checks of QCSim's own tests: Deutsch-Jozsa (DeutschJozsaTests.cpp),
+Simon (SimonAlgorithm.h:167-248), superdense coding (Tests.cpp:279-301), teleportation and entanglement
+swapping (TeleportationTests.cpp, approxEqual at 1e-10) and quantum counting (Tests.cpp:619-663).  The
+counting circuit's final state is also compared with the CPU oracle (1e-12)."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def Q():
+    import qcsim_gb300
+    from qcsim_gb300 import _lib
+    try:
+        _lib.load()
+    except _lib.EngineUnavailable as e:
+        pytest.fail(f"engine not built: {e}")
+    return qcsim_gb300
+
+
+@pytest.mark.parametrize("N", [2, 3, 5, 9])
+def test_deutsch_jozsa(Q, N):
+    from qcsim_gb300 import algorithms as A
+    FT = A.DeutschJozsaAlgorithm.FunctionType
+    dj = A.DeutschJozsaAlgorithm(N, seed=N, function_seed=N)
+    for i in range(15):
+        ft = FT.constantZero if i < 5 else FT.constantOne if i < 10 else FT.balanced
+        dj.setFunction(ft)
+        assert dj.WasConstantResult(dj.Execute()) == (ft != FT.balanced), (N, i)
+    dj.close()
+
+
+@pytest.mark.parametrize("N", [2, 3, 4])
+def test_simon(Q, N):
+    from qcsim_gb300 import algorithms as A
+    simon = A.SimonAlgorithm(N, seed=7, function_seed=N)
+    for s in range(1 << N):
+        simon.setString(s)
+        assert simon.f.checkFunction()
+        assert simon.Execute() == s, (N, s)
+    simon.close()
+
+
+def test_superdense_coding(Q):
+    from qcsim_gb300 import teleportation as T
+    coding = T.SuperdenseCoding(seed=3)
+    for bit1 in (False, True):
+        for bit2 in (False, True):
+            for _ in range(3):
+                coding.SetBits(bit1, bit2)
+                got = coding.Execute()
+                assert (bool(got & 1), bool(got & 2)) == (bit1, bit2)
+    coding.close()
+
+
+def _random_qubit_state(rng):
+    a = complex(*rng.uniform(-1, 1, 2))
+    b = complex(*rng.uniform(-1, 1, 2))
+    n = np.sqrt(abs(a) ** 2 + abs(b) ** 2)
+    return a / n, b / n
+
+
+def test_teleportation(Q):
+    """TeleportationTests (TeleportationTests.cpp:120-170): basis states arrive as measured; a generic state
+    arrives on qubit 2 next to the two measured bits, with explicit and with coherent correction"""
+    from qcsim_gb300 import teleportation as T
+    rng = np.random.default_rng(5)
+    qt = T.QuantumTeleportationRealization(seed=11)
+    for i in range(12):
+        up = bool(i % 2)
+        qt.SetState(0, 1) if up else qt.SetState(1, 0)
+        assert qt.Execute() == int(up)
+    for i in range(16):
+        alpha, beta = _random_qubit_state(rng)
+        qt.SetState(alpha, beta)
+        bits = qt.Teleport(i >= 8)
+        assert abs(qt.getBasisStateAmplitude(bits) - alpha) < 1e-10
+        assert abs(qt.getBasisStateAmplitude(4 | bits) - beta) < 1e-10
+    qt.close()
+
+
+def test_teleport_sub_algorithm(Q):
+    """TeleportTests (TeleportationTests.cpp:9-72): QC::SubAlgo::Teleport over a bare register"""
+    from qcsim_gb300 import QubitRegister
+    from qcsim_gb300 import teleportation as T
+    rng = np.random.default_rng(6)
+    tp = T.Teleport()
+    reg = QubitRegister(3, seed=13)
+    for i in range(10):
+        reg.setToBasisState(i % 2)
+        tp.Execute(reg)
+        assert reg.MeasureQubit(2) == i % 2
+    for _ in range(16):
+        alpha, beta = _random_qubit_state(rng)
+        reg.Clear()
+        reg.setRawAmplitude(0, alpha)
+        reg.setRawAmplitude(1, beta)
+        reg.Normalize()
+        bits = tp.Execute(reg)
+        assert abs(reg.getBasisStateAmplitude(bits) - alpha) < 1e-10
+        assert abs(reg.getBasisStateAmplitude(4 | bits) - beta) < 1e-10
+    reg.close()
+
+
+def test_entanglement_swapping(Q):
+    """EntanglementSwappingTests (TeleportationTests.cpp:74-118): the Bell pair sent on (0, 2) ends on (4, 5)"""
+    from qcsim_gb300 import QubitRegister
+    from qcsim_gb300 import teleportation as T
+    es = T.EntanglementSwapping(seed=17)
+    bell = T.BellState()
+    reg = QubitRegister(2, seed=1)
+    for i in range(16):
+        s1, s2 = bool(i & 1), bool(i & 2)
+        bell.setBellState(reg, 0, 1, s1, s2)
+        es.SetBellStateToBeSent(s1, s2)
+        meas = es.Teleport(i >= 8)
+        v = es.getRegisterStorage()
+        expect = reg.getRegisterStorage()
+        for state in range(64):
+            want = expect[state >> 4] if (state & 0xF) == meas else 0
+            assert abs(v[state] - want) < 1e-10, (i, state)
+    es.close()
+    reg.close()
+
+
+def test_quantum_counting_state_matches_oracle(Q):
+    """the 14-qubit counting register (6 precision, 4 Grover qubits, 5 marked states) after the controlled
+    Grover iterations and the inverse QFT, against the CPU oracle"""
+    from oracle import bind as B
+    from qcsim_gb300 import counting as C
+    qc = C.QuantumCountingAlgorithm(6, 4, seed=2)
+    qc.SetMarkedStates([1, 4, 7, 10, 13])
+    ref = B.OracleRegister(14)
+    ref.apply(qc.circuit())
+    assert B.oracle().qo_qft(ref.h, 0, 5, 1, 0) == 0
+    qc.ExecuteWithoutMeasurement()
+    assert np.max(np.abs(qc.getRegisterStorage() - ref.state())) < 1e-12
+    qc.close()
+
+
+def test_quantum_counting(Q):
+    """CountingTests (Tests.cpp:619-663): for 0..16 marked states of 4 Grover qubits, the most measured value of
+    the 6 precision qubits (10000 shots) gives the number of marked states"""
+    from qcsim_gb300 import counting as C
+    rng = np.random.default_rng(9)
+    for marked in range(17):
+        qc = C.QuantumCountingAlgorithm(6, 4, seed=marked)
+        qc.SetMarkedStates(rng.permutation(16)[:marked].tolist())
+        res = qc.ExecuteWithMultipleMeasurements(10000)
+        state = max(res.items(), key=lambda kv: kv[1])[0]
+        assert qc.GetCountForState(state) == marked, (marked, res)
+        qc.close()
