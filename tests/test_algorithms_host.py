@@ -159,3 +159,28 @@ def test_quantum_counting_circuit_on_the_oracle(monkeypatch):
         assert p[np.arange(p.size) >> (P + Gq) != 0].sum() < 1e-20
         px = np.bincount(np.arange(p.size) & ((1 << P) - 1), weights=p)
         assert qc.GetCountForState(int(np.argmax(px))) == marked
+
+
+def test_operator_basis_change():
+    """MeasurementBasis::switchToOperatorBasis (Utils.h:143-205): the unitary diagonalises the operator with the
+    larger eigenvalue first; Z gives the identity, -Z the swap, and switchBack the adjoint"""
+    from qcsim_gb300.measurement_basis import MeasurementBasis as MB
+    z = np.diag([1.0, -1.0]).astype(np.complex128)
+    x = np.array([[0, 1], [1, 0]], dtype=np.complex128)
+    y = np.array([[0, -1j], [1j, 0]])
+    assert np.array_equal(MB.operatorBasisMatrix(z), np.eye(2))
+    assert np.array_equal(MB.operatorBasisMatrix(-z), np.array([[0, 1], [1, 0]]))
+    rng = np.random.default_rng(3)
+    ops = [x, y, (-z - x) / np.sqrt(2), (z - x) / np.sqrt(2)]
+    for _ in range(20):
+        a, b = rng.standard_normal(2)
+        c = complex(*rng.standard_normal(2))
+        ops.append(np.array([[a, c], [np.conj(c), b]]))
+    for op in ops:
+        U = MB.operatorBasisMatrix(op)
+        assert np.abs(U @ U.conj().T - np.eye(2)).max() < 1e-14
+        d = U @ op @ U.conj().T
+        ev = np.linalg.eigvalsh(op)
+        assert abs(d[0, 1]) < 1e-12 and abs(d[1, 0]) < 1e-12
+        assert abs(d[0, 0] - ev[1]) < 1e-12 and abs(d[1, 1] - ev[0]) < 1e-12
+        assert np.array_equal(MB.operatorBasisMatrix(op, True), U.conj().T)

@@ -1,8 +1,9 @@
 """QCSim's oracle algorithms, teleportation family and quantum counting over the engine, through the Python
 mirror of their classes, with the checks of QCSim's own tests: Deutsch-Jozsa (DeutschJozsaTests.cpp),
 Simon (SimonAlgorithm.h:167-248), superdense coding (Tests.cpp:279-301), teleportation and entanglement
-swapping (TeleportationTests.cpp, approxEqual at 1e-10) and quantum counting (Tests.cpp:619-663).  The
-counting circuit's final state is also compared with the CPU oracle (1e-12)."""
+swapping (TeleportationTests.cpp, approxEqual at 1e-10), quantum counting (Tests.cpp:619-663), the
+statevector expectation values (Tests.cpp:665-723), the CHSH inequality (Tests.cpp:303-330) and BB84
+(Tests.cpp:474-520).  The counting circuit's final state is also compared with the CPU oracle (1e-12)."""
 import numpy as np
 import pytest
 
@@ -152,3 +153,92 @@ def test_quantum_counting(Q):
         state = max(res.items(), key=lambda kv: kv[1])[0]
         assert qc.GetCountForState(state) == marked, (marked, res)
         qc.close()
+
+
+def test_expectation_values_statevector(Q):
+    """checkExpectationValuesStatevector (Tests.cpp:665-723): <I> = 1, <Z0> = 1, -1 after X, 0 after H, <Z1> = 0"""
+    from qcsim_gb300 import gates as G
+    reg = Q.QubitRegister(3, seed=1)
+    z0 = [G.AppliedGate(G.PauliZGate().getRawOperatorMatrix(), 0)]
+    assert abs(reg.ExpectationValue([]) - 1.0) <= 1e-6
+    assert abs(reg.ExpectationValue(z0) - 1.0) <= 1e-6
+    reg.ApplyGate(G.PauliXGate(), 0)
+    assert abs(reg.ExpectationValue(z0) + 1.0) <= 1e-6
+    reg.ApplyGate(G.HadamardGate(), 0)
+    assert abs(reg.ExpectationValue(z0)) <= 1e-6
+    reg.setToBasisState(0)
+    reg.ApplyGate(G.HadamardGate(), 1)
+    assert abs(reg.ExpectationValue([G.AppliedGate(G.PauliZGate().getRawOperatorMatrix(), 1)])) <= 1e-6
+    reg.close()
+
+
+@pytest.mark.parametrize("separate", [False, True])
+def test_chsh_inequality(Q, separate):
+    """BellInequalitiesTests (Tests.cpp:303-330): the CHSH value exceeds 2 and lies within 0.1 of 2 sqrt(2)
+    (20000 checks per run here, 100000 in the reference)"""
+    from qcsim_gb300 import measurement_basis as M
+    chsh = M.CheckCHSHInequality(seed=21 + separate, choice_seed=5)
+    for _ in range(20000):
+        chsh.Check(separate)
+    v = chsh.getValue()
+    assert v > 2.0 and abs(v - 2.0 * np.sqrt(2.0)) <= 0.1, v
+    chsh.close()
+
+
+def test_bb84(Q):
+    """QuantumCryptograpyTests (Tests.cpp:474-520): without eavesdropping the compared bits match and so do the
+    keys; with an eavesdropper on every bit or on random bits the comparison fails"""
+    from qcsim_gb300 import measurement_basis as M
+    bb84 = M.BB84Protocol(seed=3, choice_seed=4)
+    for i in range(30):
+        eavesdrop = i > 9
+        bb84.setEavesdropping(eavesdrop)
+        bb84.setRandomEavesdropping(i > 19)
+        match = bb84.Execute()
+        assert bool(match) != eavesdrop, i
+        if match:
+            assert bb84.compareKeys() and len(bb84.getReceivedKey()) > 64
+    bb84.close()
+
+
+def _two_qubit_state(rng):
+    v = rng.uniform(-1, 1, 4) + 1j * rng.uniform(-1, 1, 4)
+    return v / np.linalg.norm(v)
+
+
+def test_distributed_cnot(Q):
+    """distributedCNOTTest (DistributedTests.cpp:8-100): the control on qubit 0 and target on qubit 3 end as
+    after a local CNOT, next to the measured Bell-pair qubits"""
+    from qcsim_gb300 import distributed as D
+    rng = np.random.default_rng(8)
+    dc = D.DistributedCNOT(seed=5)
+    for _ in range(16):
+        a = _two_qubit_state(rng)  # index bit 0 = control, bit 1 = target
+        dc.Clear()
+        for idx, amp in zip((0, 1, 8, 9), a):
+            dc.setRawAmplitude(idx, amp)
+        dc.Normalize()
+        m = dc.Execute() << 1
+        want = a[[0, 3, 2, 1]]  # CNOT(target <- control)
+        got = [dc.getBasisStateAmplitude(s) for s in (m, m | 1, 8 | m, 8 | m | 1)]
+        assert np.abs(np.array(got) - want).max() < 1e-10
+    dc.close()
+
+
+def test_teleported_cnot(Q):
+    """teleportedCNOTTest (DistributedTests.cpp:102-190): target on qubit 0, control on qubit 5, the CNOT's
+    result on qubits 2 (target) and 3 (control) next to the measured bits"""
+    from qcsim_gb300 import distributed as D
+    rng = np.random.default_rng(9)
+    tc = D.TeleportedCNOT(seed=6)
+    for _ in range(16):
+        a = _two_qubit_state(rng)  # index bit 0 = target, bit 1 = control
+        tc.Clear()
+        for idx, amp in zip((0, 1, 0x20, 0x21), a):
+            tc.setRawAmplitude(idx, amp)
+        tc.Normalize()
+        m = tc.Execute()
+        want = a[[0, 1, 3, 2]]
+        v = tc.getRegisterStorage()
+        assert np.abs(np.array([v[(i << 2) | m] for i in range(4)]) - want).max() < 1e-10
+    tc.close()

@@ -1,0 +1,114 @@
+"""The small-protocol mirrors run end to end on the CPU, no GPU: each algorithm's register is replaced by a
+stand-in over the oracle (tests/oracle_register.py), so the host logic (gate order, mid-circuit measurement
+handling, classical corrections, bookkeeping) is checked against QCSim's own test conditions.  The same
+checks run over the engine in test_gpu_protocols.py."""
+import numpy as np
+import pytest
+
+from oracle_register import OracleBackedRegister
+from qcsim_gb300 import algorithms as A
+
+
+@pytest.fixture
+def on_oracle(monkeypatch):
+    monkeypatch.setattr(A, "QubitRegister", OracleBackedRegister)
+
+
+def test_deutsch_jozsa_and_simon(on_oracle):
+    FT = A.DeutschJozsaAlgorithm.FunctionType
+    for N in (2, 4):
+        dj = A.DeutschJozsaAlgorithm(N, seed=N, function_seed=N)
+        for ft in (FT.constantZero, FT.constantOne, FT.balanced, FT.balanced):
+            dj.setFunction(ft)
+            assert dj.WasConstantResult(dj.Execute()) == (ft != FT.balanced)
+    simon = A.SimonAlgorithm(3, seed=1, function_seed=3)
+    for s in (0, 3, 5):
+        simon.setString(s)
+        assert simon.Execute() == s
+
+
+def test_teleportation_family(on_oracle):
+    from qcsim_gb300 import teleportation as T
+    rng = np.random.default_rng(2)
+    qt = T.QuantumTeleportationRealization(seed=1)
+    for explicit in (False, True):
+        for _ in range(4):
+            a, b = rng.standard_normal(2) + 1j * rng.standard_normal(2)
+            n = np.sqrt(abs(a) ** 2 + abs(b) ** 2)
+            qt.SetState(a / n, b / n)
+            bits = qt.Teleport(explicit)
+            assert abs(qt.getBasisStateAmplitude(bits) - a / n) < 1e-12
+            assert abs(qt.getBasisStateAmplitude(4 | bits) - b / n) < 1e-12
+    reg = OracleBackedRegister(3, seed=4)
+    tp = T.Teleport()
+    for v in (0, 1, 1, 0):
+        reg.setToBasisState(v)
+        tp.Execute(reg)
+        assert reg.MeasureQubit(2) == v
+    es = T.EntanglementSwapping(seed=3)
+    ref = OracleBackedRegister(2, seed=0)
+    for i in range(4):
+        T.BellState().setBellState(ref, 0, 1, bool(i & 1), bool(i & 2))
+        es.SetBellStateToBeSent(bool(i & 1), bool(i & 2))
+        meas = es.Teleport(bool(i & 1))
+        v, want = es.getRegisterStorage(), ref.getRegisterStorage()
+        assert all(abs(v[s] - (want[s >> 4] if (s & 15) == meas else 0)) < 1e-12 for s in range(64))
+    coding = T.SuperdenseCoding(seed=5)
+    for b1 in (False, True):
+        for b2 in (False, True):
+            coding.SetBits(b1, b2)
+            got = coding.Execute()
+            assert (bool(got & 1), bool(got & 2)) == (b1, b2)
+
+
+def test_distributed_cnots(on_oracle):
+    from qcsim_gb300 import distributed as D
+    rng = np.random.default_rng(7)
+    dc, tc = D.DistributedCNOT(seed=1), D.TeleportedCNOT(seed=2)
+    for _ in range(6):
+        a = rng.standard_normal(4) + 1j * rng.standard_normal(4)
+        a /= np.linalg.norm(a)
+        dc.Clear()
+        for idx, amp in zip((0, 1, 8, 9), a):
+            dc.setRawAmplitude(idx, amp)
+        dc.Normalize()
+        m = dc.Execute() << 1
+        got = [dc.getBasisStateAmplitude(s) for s in (m, m | 1, 8 | m, 8 | m | 1)]
+        assert np.abs(np.array(got) - a[[0, 3, 2, 1]]).max() < 1e-12
+        tc.Clear()
+        for idx, amp in zip((0, 1, 0x20, 0x21), a):
+            tc.setRawAmplitude(idx, amp)
+        tc.Normalize()
+        m = tc.Execute()
+        v = tc.getRegisterStorage()
+        assert np.abs(np.array([v[(i << 2) | m] for i in range(4)]) - a[[0, 1, 3, 2]]).max() < 1e-12
+
+
+def test_chsh_and_bb84(on_oracle):
+    from qcsim_gb300 import measurement_basis as M
+    chsh = M.CheckCHSHInequality(seed=3, choice_seed=4)
+    for separate in (False, True):
+        chsh.ResetStatistics()
+        for _ in range(4000):
+            chsh.Check(separate)
+        v = chsh.getValue()
+        assert v > 2.0 and abs(v - 2 * np.sqrt(2)) < 0.2, v
+    bb84 = M.BB84Protocol(seed=5, nrBits=256, choice_seed=6)
+    for eavesdrop, rand in ((False, False), (True, False), (True, True)):
+        bb84.setEavesdropping(eavesdrop)
+        bb84.setRandomEavesdropping(rand)
+        match = bb84.Execute()
+        assert bool(match) != eavesdrop
+        if match:
+            assert bb84.compareKeys() and bb84.getReceivedKey() == bb84.getSentKey()
+
+
+def test_quantum_counting_execute(on_oracle):
+    """Execute end to end (circuit, inverse QFT on the precision qubits through the QFT mirror, measurement)"""
+    from qcsim_gb300 import counting as C
+    qc = C.QuantumCountingAlgorithm(5, 2, seed=1)
+    for marked in ([], [1], [0, 3], [0, 1, 2, 3]):
+        qc.SetMarkedStates(marked)
+        res = qc.ExecuteWithMultipleMeasurements(2000)
+        state = max(res.items(), key=lambda kv: kv[1])[0]
+        assert qc.GetCountForState(state) == len(marked)
