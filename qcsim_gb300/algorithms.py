@@ -6,8 +6,9 @@ gates NQubitsQuantumGate (NQubitsQuantumGate.h:9-78) / NQubitsControlledQuantumG
 (NQubitsControlledQuantumGate.h:9-97), phase estimation (PhaseEstimation.h:11-231), Grover's search
 with the diagonal oracle matrix (GroverAlgorithm.h:14-124), Bernstein-Vazirani with its diagonal oracle
 (BernsteinVazirani.h:14-106), Deutsch-Jozsa (DeutschJozsa.h:16-137) and Simon's algorithm (SimonAlgorithm.h:15-248)
-with their permutation oracles, the QFT adders DraperAdder / DraperAdderWithCarry (DraperAdder.h:11-117) and the
-three-qubit flip and sign codes (ErrorCorrectionBase.h, ErrorCorrection3Qubits.h), and Shor's factoring with
+with their permutation oracles, the QFT adders DraperAdder / DraperAdderWithCarry (DraperAdder.h:11-117), the ripple-carry qubit
+adders (QuantumAdder.h), the three-qubit flip and sign codes (ErrorCorrectionBase.h, ErrorCorrection3Qubits.h) and
+the nine-qubit Shor code (ShorCode.h), and Shor's factoring with
 the tensor-product period finding (ShorAlgorithm.h:15-296, PhaseEstimation.h:100-149).
 
 The QFT runs as one engine call (qcs_qft), which applies the reference's gate sequence; the one-qubit
@@ -489,6 +490,63 @@ class DraperAdderWithCarry(DraperAdder):
         self.fourier.IQFT(self.reg, False)
 
 
+class TwoQubitsHalfAdder:
+    """Adders::TwoQubitsHalfAdder (QuantumAdder.h:10-43): sum of qubit1 and qubit2 into qubit2, carry into aux
+    (Toffoli, then CNOT); returns 1 for a qubit out of range and 2 for repeated qubits"""
+
+    def __init__(self, qubit1: int, qubit2: int, qubitaux: int):
+        self.q1, self.q2, self.aux = qubit1, qubit2, qubitaux
+        self.toffoli, self.cnot = G.ToffoliGate(), G.CNOTGate()
+
+    def Execute(self, reg) -> int:
+        n = reg.getNrQubits()
+        if self.aux >= n or self.q2 >= n or self.q1 >= n:
+            return 1
+        if len({self.q1, self.q2, self.aux}) < 3:
+            return 2
+        reg.ApplyGates([(self.toffoli, self.aux, self.q1, self.q2), (self.cnot, self.q2, self.q1)])
+        return 0
+
+
+class TwoQubitsFullAdder(TwoQubitsHalfAdder):
+    """Adders::TwoQubitsFullAdder (QuantumAdder.h:45-85): two half adders and a CNOT that restores qubit2; the
+    sum ends on cin and the carry on aux"""
+
+    def __init__(self, qubit1: int, qubit2: int, cin: int, qubitaux: int):
+        super().__init__(qubit1, qubit2, qubitaux)
+        self.ci = cin
+        self.halfAdder = TwoQubitsHalfAdder(qubit2, cin, qubitaux)
+
+    def Execute(self, reg) -> int:
+        n = reg.getNrQubits()
+        if self.aux >= n or self.q2 >= n or self.q1 >= n or self.ci >= n:
+            return 1
+        if len({self.q1, self.q2, self.aux, self.ci}) < 4:
+            return 2
+        super().Execute(reg)
+        self.halfAdder.Execute(reg)
+        reg.ApplyGate(self.cnot, self.q2, self.q1)
+        return 0
+
+
+class NQubitsAdderAlgorithm(QuantumAlgorithm):
+    """Adders::NQubitsAdderAlgorithm (QuantumAdder.h:87-125): 3N + 1 qubits, the addends on qubits 0..N-1 and
+    N..2N-1 (kept), a ripple of full adders leaving the N + 1-bit sum on qubits 2N..3N; returns the measured
+    register"""
+
+    def __init__(self, N: int = 3, addseed: int = 0, **kw):
+        super().__init__(3 * N + 1, addseed, **kw)
+        self.setToBasisState(0)
+
+    def Execute(self) -> int:
+        nq = self.getNrQubits()
+        assert nq >= 4
+        n = (nq - 1) // 3
+        for k in range(n):
+            TwoQubitsFullAdder(k, n + k, 2 * n + k, 2 * n + k + 1).Execute(self.reg)
+        return self.Measure()
+
+
 class BernsteinVaziraniOracle:
     """BernsteinVazirani::Oracle (BernsteinVazirani.h:16-57): -1 on the basis states whose bitwise product
     with the hidden string has odd parity"""
@@ -773,6 +831,59 @@ class ErrorCorrection3QubitsSign(ErrorCorrection3Qubits):
     def ApplyHadamardOnAllQubits(self) -> None:
         for i in range(self.getNrQubits()):
             self.ApplyGate(self.hadamard, i)
+
+
+class ShorCode(ErrorCorrectionBase):
+    """ErrorCorrection::ShorCode (ShorCode.h:8-107): the nine-qubit code; any single-qubit flip, sign or
+    combined (iY) error on one of the nine qubits is corrected.  Execute returns the measurement of qubits
+    1-8, which is 0 exactly when no error was applied."""
+
+    class ErrorType(enum.IntEnum):
+        Flip = 0
+        Sign = 1
+        Both = 2
+        none = 3  # the reference's None: no error
+
+    def __init__(self, addseed: int = 0, **kw):
+        super().__init__(9, addseed, **kw)
+        self.errorType = self.ErrorType.Flip
+        self.hadamard = G.HadamardGate()
+        self.z = G.PauliZGate()
+        self.iy = G.SingleQubitGate(1j * G.PauliYGate().getRawOperatorMatrix())
+
+    def setErrorType(self, t) -> None:
+        self.errorType = self.ErrorType(t)
+
+    def getErrorType(self):
+        return self.errorType
+
+    def Execute(self) -> int:
+        self.Encode()
+        self.ApplyError()
+        self.DetectAndCorrect()
+        return self.Measure(1, self.getNrQubits() - 1)
+
+    def ApplyError(self) -> None:
+        if self.errorQubit >= self.getNrQubits():
+            return
+        gate = {self.ErrorType.Flip: self.x, self.ErrorType.Sign: self.z, self.ErrorType.Both: self.iy}.get(self.errorType)
+        if gate is not None:
+            self.ApplyGate(gate, self.errorQubit)
+
+    def Encode(self) -> None:
+        """ShorCode.h:66-80: the sign code across qubits 0, 3, 6, each expanded into a flip code"""
+        ops = [(self.cnot, 3, 0), (self.cnot, 6, 0)]
+        for q in (0, 3, 6):
+            ops += [(self.hadamard, q), (self.cnot, q + 1, q), (self.cnot, q + 2, q)]
+        self.ApplyGates(ops)
+
+    def DetectAndCorrect(self) -> None:
+        """ShorCode.h:82-98"""
+        ops = []
+        for q in (0, 3, 6):
+            ops += [(self.cnot, q + 1, q), (self.cnot, q + 2, q), (self.ccnot, q, q + 1, q + 2), (self.hadamard, q)]
+        ops += [(self.cnot, 3, 0), (self.cnot, 6, 0), (self.ccnot, 0, 3, 6)]
+        self.ApplyGates(ops)
 
 
 class FxBase:

@@ -112,3 +112,105 @@ def test_quantum_counting_execute(on_oracle):
         res = qc.ExecuteWithMultipleMeasurements(2000)
         state = max(res.items(), key=lambda kv: kv[1])[0]
         assert qc.GetCountForState(state) == len(marked)
+
+
+def _check_shor_code(make, rng, states=4):
+    """ShorCodeTests (ErrorCorrectionTests.cpp:150-205): every error type on every qubit is corrected; the
+    measurement of qubits 1-8 is non-zero exactly when an error was applied, and qubit 0 carries the state"""
+    code = make()
+    ET = type(code).ErrorType
+    for _ in range(states):
+        a, b = rng.uniform(-1, 1, 2) + 1j * rng.uniform(-1, 1, 2)
+        n = np.sqrt(abs(a) ** 2 + abs(b) ** 2)
+        a, b = a / n, b / n
+        for q in range(10):
+            code.SetErrorQubit(q)
+            for c in range(3):
+                code.SetState(a, b)
+                code.setErrorType(ET.none if q == 9 else ET(c))
+                res = code.Execute()
+                assert (res != 0) == (q != 9), (q, c, res)
+                v = code.getRegisterStorage()
+                assert abs(np.conj(a) * v[res << 1] + np.conj(b) * v[(res << 1) | 1]) ** 2 >= 0.99999, (q, c)
+                if q == 9:
+                    break
+    code.close()
+
+
+def _check_qubit_adders(make_reg, make_adder, rng):
+    """quantumHalfAdderTests / quantumFullAdderTests / NQubitsAdderTests (AdderTests.cpp:9-150)"""
+    reg = make_reg(3)
+    half = A.TwoQubitsHalfAdder(0, 1, 2)
+    for x in range(4):
+        reg.setToBasisState(x)
+        assert half.Execute(reg) == 0
+        res = reg.MeasureAll()
+        assert res & 1 == x & 1 and res >> 1 == (x & 1) + (x >> 1)
+    reg = make_reg(4)
+    full = A.TwoQubitsFullAdder(0, 1, 2, 3)
+    for x in range(4):
+        reg.setToBasisState(x)
+        assert full.Execute(reg) == 0
+        res = reg.MeasureAll()
+        assert res & 3 == x and res >> 2 == (x & 1) + (x >> 1)
+    assert A.TwoQubitsHalfAdder(0, 0, 2).Execute(reg) == 2 and A.TwoQubitsFullAdder(0, 1, 2, 9).Execute(reg) == 1
+    adder = make_adder()
+    for _ in range(10):
+        n1, n2 = (int(v) for v in rng.integers(0, 8, 2))
+        adder.setToBasisState((n2 << 3) | n1)
+        res = adder.Execute()
+        assert res & 0x3F == (n2 << 3) | n1 and res >> 6 == n1 + n2
+    adder.close()
+
+
+def test_shor_code_and_adders(on_oracle):
+    rng = np.random.default_rng(12)
+    _check_shor_code(lambda: A.ShorCode(seed=2), rng, states=2)
+    _check_qubit_adders(lambda n: OracleBackedRegister(n, seed=1), lambda: A.NQubitsAdderAlgorithm(3, seed=3), rng)
+
+
+def _check_paradoxes(P, hardy_step=0.1):
+    """ParadoxesTests (ParadoxesTests.cpp) and CoinFlippingTests (GamesTests.cpp:9-26): the eraser's four and two
+    outcomes within 5 % of their expected counts, the bomb's efficiency and Hardy's gamma within 0.08 of the
+    formulas, and the coin always back on heads"""
+    import math
+    er = P.QuantumEraser(seed=1)
+    m = er.ExecuteWithMultipleMeasurements(100000)
+    assert all(abs(m.get(k, 0) - 25000) <= 1250 for k in range(4)), m
+    er.setEraser()
+    m = er.ExecuteWithMultipleMeasurements(100000)
+    assert abs(m.get(0, 0) - 50000) <= 2500 and abs(m.get(3, 0) - 50000) <= 2500
+    assert m.get(1, 0) == 0 and m.get(2, 0) == 0
+    er.close()
+    bomb = P.GeneralElitzurVaidmanBomb(4, seed=2)
+    for stages in range(1, 5):
+        bomb.setStages(stages)
+        theta = 0.05 * math.pi
+        while theta < 0.9 * math.pi:
+            bomb.setTheta(theta)
+            m = bomb.ExecuteWithMultipleMeasurements(10000)
+            result = m.get(0, 0) / (10000 - m.get(1, 0))
+            assert abs(result - bomb.TheoreticalEfficiency()) <= 0.08, (stages, theta)
+            theta += 0.05 * math.pi
+    bomb.close()
+    hardy = P.HardyParadox(seed=3)
+    t0 = hardy_step * math.pi
+    while t0 < math.pi - hardy_step * math.pi:
+        hardy.setTheta0(t0)
+        t1 = hardy_step * math.pi
+        while t1 < math.pi - hardy_step * math.pi:
+            hardy.setTheta1(t1)
+            m = hardy.ExecuteWithMultipleMeasurements(100000)
+            p = [m.get(k, 0) / 100000 for k in range(4)]
+            assert abs(p[0] / sum(p) - hardy.TheoreticalGamma()) <= 0.08, (t0, t1)
+            t1 += hardy_step * math.pi
+        t0 += hardy_step * math.pi
+    hardy.close()
+    coin = P.CoinFlipping(seed=4, choice_seed=5)
+    assert all(coin.Execute() == 0 for _ in range(100))
+    coin.close()
+
+
+def test_paradoxes_and_coin_flipping(on_oracle):
+    from qcsim_gb300 import paradoxes as P
+    _check_paradoxes(P, hardy_step=0.1)
