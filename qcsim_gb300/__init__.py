@@ -3,6 +3,21 @@
 The engine is libqcs_gpu.so (CUDA, sm_103a) behind the C ABI of include/qcs_gpu.h.  This package holds
 the host-side mirror of the reference interface (QubitRegister, the QC::Gates classes, the QFT and
 one-qubit-transform sub-algorithms), the seeded workload generators and the build recipe.
+
+Mirrors of QCSim's algorithm classes over the engine, by module:
+  algorithms         QuantumAlgorithm, QFT, phase estimation, Grover, Bernstein-Vazirani, Deutsch-Jozsa, Simon,
+                     the adders, the error-correction codes, Shor's factoring
+  vqe                VQE with Pauli-string terms and its Nelder-Mead search
+  ising              IsingModel and the QAOA sub-algorithm with its optimiser (one register)
+  qaoa               many QAOA instances batched in one persistent launch
+  counting           quantum counting and the n-controlled NOT with ancillas
+  teleportation      cat entangler / disentangler, Bell states, teleportation, entanglement swapping,
+                     superdense coding
+  measurement_basis  basis changes, the CHSH check, BB84
+  distributed        distributed and teleported CNOTs
+  paradoxes          quantum eraser, Hardy's paradox, the Elitzur-Vaidman bomb, coin flipping
+  schrodinger        the split-operator Schrodinger simulation
+  costmodel          the learned fusion cost model
 """
 from . import gates
 from ._lib import EngineUnavailable, QcsError
