@@ -354,3 +354,34 @@ def test_paradoxes_and_coin_flipping(Q):
     """the reference's Hardy sweep steps both angles by 0.025 pi"""
     from qcsim_gb300 import paradoxes as P
     _check_paradoxes(P, hardy_step=0.025)
+
+
+def _check_gate_oracles(O):
+    """DeutschWithGatesTests (DeutschJozsaTests.cpp:8-47) and its N-qubit form, the Bernstein-Vazirani and Simon
+    algorithms with gate-built oracles (SimonWithGatesTests, Tests.cpp:522-560): the same answers as with the
+    oracle matrices"""
+    FT = O.DeutschJozsaAlgorithmWithGatesOracle.FunctionType
+    for N in (2, 3, 5, 6):
+        dj = O.DeutschJozsaAlgorithmWithGatesOracle(N, seed=N, function_seed=N)
+        for i in range(9):
+            ft = FT.constantZero if i < 3 else FT.constantOne if i < 6 else FT.balanced
+            dj.setFunction(ft)
+            assert dj.WasConstantResult(dj.Execute()) == (ft != FT.balanced), (N, i)
+        dj.close()
+    for N in (2, 3, 5):
+        bv = O.BernsteinVaziraniAlgorithmWithGatesOracle(N, seed=N)
+        for s in range(1 << N):
+            bv.setString(s)
+            assert bv.Execute() == s, (N, s)
+        bv.close()
+    for N in (2, 3, 4):
+        simon = O.SimonAlgorithmWithGatesOracle(N, seed=N, function_seed=N)
+        for s in range(1 << N):
+            simon.setString(s)
+            assert simon.Execute() == s, (N, s)
+        simon.close()
+
+
+def test_gate_built_oracles(Q):
+    from qcsim_gb300 import oracles as O
+    _check_gate_oracles(O)

@@ -214,3 +214,59 @@ def _check_paradoxes(P, hardy_step=0.1):
 def test_paradoxes_and_coin_flipping(on_oracle):
     from qcsim_gb300 import paradoxes as P
     _check_paradoxes(P, hardy_step=0.1)
+
+
+def _check_gate_oracles(O):
+    """DeutschWithGatesTests (DeutschJozsaTests.cpp:8-47) and its N-qubit form, the Bernstein-Vazirani and Simon
+    algorithms with gate-built oracles (SimonWithGatesTests, Tests.cpp:522-560): the same answers as with the
+    oracle matrices"""
+    FT = O.DeutschJozsaAlgorithmWithGatesOracle.FunctionType
+    for N in (2, 3, 5, 6):
+        dj = O.DeutschJozsaAlgorithmWithGatesOracle(N, seed=N, function_seed=N)
+        for i in range(9):
+            ft = FT.constantZero if i < 3 else FT.constantOne if i < 6 else FT.balanced
+            dj.setFunction(ft)
+            assert dj.WasConstantResult(dj.Execute()) == (ft != FT.balanced), (N, i)
+        dj.close()
+    for N in (2, 3, 5):
+        bv = O.BernsteinVaziraniAlgorithmWithGatesOracle(N, seed=N)
+        for s in range(1 << N):
+            bv.setString(s)
+            assert bv.Execute() == s, (N, s)
+        bv.close()
+    for N in (2, 3, 4):
+        simon = O.SimonAlgorithmWithGatesOracle(N, seed=N, function_seed=N)
+        for s in range(1 << N):
+            simon.setString(s)
+            assert simon.Execute() == s, (N, s)
+        simon.close()
+
+
+def test_gate_built_oracles(on_oracle):
+    from qcsim_gb300 import oracles as O
+    _check_gate_oracles(O)
+
+
+def test_n_controlled_gates_with_ancilla():
+    """NControlledGateWithAncilla.h:23-75: with 1 to 7 controls, two NOTs added as controlled gates flip their
+    targets exactly when every control is set, and the ancillas return to 0"""
+    from qcsim_gb300 import counting as C
+    from qcsim_gb300 import gates as G
+    from qcsim_gb300 import oracles as O
+    x = G.PauliXGate().getRawOperatorMatrix()
+    for nc in range(1, 8):
+        g = O.NControlledGatesWithAncilla()
+        g.SetControlQubits(range(nc))
+        g.SetStartAncillaQubits(nc + 2)
+        assert g.AddGate(G.AppliedGate(x, nc)) and g.AddGate(G.AppliedGate(x, nc + 1))
+        seq = C.GateSequence()
+        g.Execute(seq)
+        for c in range(1 << nc):
+            bits = c
+            for gate, t, c1, c2 in seq.ops:
+                k = gate.getQubitsNumber()
+                if (k == 3 and (bits >> c1) & (bits >> c2) & 1) or (k == 2 and (bits >> c1) & 1):
+                    bits ^= 1 << t
+            assert bits >> (nc + 2) == 0, (nc, c)
+            full = c == (1 << nc) - 1
+            assert (bits >> nc) & 3 == (3 if full else 0), (nc, c)
