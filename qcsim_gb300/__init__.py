@@ -16,6 +16,7 @@ Mirrors of QCSim's algorithm classes over the engine, by module:
   measurement_basis  basis changes, the CHSH check, BB84
   distributed        distributed and teleported CNOTs
   paradoxes          quantum eraser, Hardy's paradox, the Elitzur-Vaidman bomb, coin flipping
+  oracles            gate-built oracles and the Deutsch-Jozsa, Bernstein-Vazirani and Simon variants on them
   schrodinger        the split-operator Schrodinger simulation
   costmodel          the learned fusion cost model
 """

@@ -611,6 +611,18 @@ def records(gates) -> np.ndarray:
     return arr
 
 
+class PreparedGates:
+    """a gate list converted once to engine records, for a circuit applied many times (QubitRegister.ApplyGates
+    takes it in place of a list); ops keeps the (gate, q0, q1, q2) tuples"""
+
+    def __init__(self, ops):
+        self.ops = [op if isinstance(op, tuple) else (op, op.getQubit1(), op.getQubit2(), op.getQubit3()) for op in ops]
+        self.recs = records(self.ops)
+
+    def __len__(self) -> int:
+        return len(self.ops)
+
+
 def cmatrix(m) -> np.ndarray:
     return np.asarray(m, dtype=np.complex128)
 

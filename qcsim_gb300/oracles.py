@@ -318,7 +318,7 @@ class SimonAlgorithmWithGatesOracle(QuantumAlgorithm):
         self.oracle.Execute(seq)
         for q in range(N):
             seq.ApplyGate(self.hadamard, q)
-        self._round = seq.ops  # the circuit of one round after the reset, rebuilt only when the string changes
+        self._round = G.PreparedGates(seq.ops)  # one round's circuit after the reset, converted once per string
 
     def Execute(self) -> int:
         N = self.getAlgoQubits() >> 1

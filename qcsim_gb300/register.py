@@ -248,15 +248,19 @@ class QubitRegister:
             self.computeGates.append(AppliedGate(m.copy(), qubit, controllingQubit1, controllingQubit2))
 
     def ApplyGates(self, gates) -> None:
-        """ApplyGates(list of AppliedGate) (QubitRegister.h:493-497); also accepts (gate, q0, q1, q2) tuples"""
-        from .gates import records
-        tuples = []
-        for g in gates:
-            if isinstance(g, tuple):
-                tuples.append(g)
-            else:
-                tuples.append((g, g.getQubit1(), g.getQubit2(), g.getQubit3()))
-        recs = records(tuples)
+        """ApplyGates(list of AppliedGate) (QubitRegister.h:493-497); also accepts (gate, q0, q1, q2) tuples, or a
+        gates.PreparedGates whose records were converted once"""
+        from .gates import PreparedGates, records
+        if isinstance(gates, PreparedGates):
+            tuples, recs = gates.ops, gates.recs
+        else:
+            tuples = []
+            for g in gates:
+                if isinstance(g, tuple):
+                    tuples.append(g)
+                else:
+                    tuples.append((g, g.getQubit1(), g.getQubit2(), g.getQubit3()))
+            recs = records(tuples)
         self.apply_records(recs)
         if self.recordGates:
             for g, *qs in tuples:

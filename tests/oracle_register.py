@@ -84,6 +84,7 @@ class OracleBackedRegister:
         self.r.apply([self._oracle_op(gate, qubit, c1, c2)])
 
     def ApplyGates(self, ops):
+        ops = getattr(ops, "ops", ops)  # a gates.PreparedGates carries its tuples
         ops = [self._oracle_op(*op) if isinstance(op, tuple) else
                self._oracle_op(op, op.getQubit1(), op.getQubit2(), op.getQubit3()) for op in ops]
         if ops:
