@@ -1,7 +1,8 @@
 """QCSim's paradox and game demonstrations over the engine: Paradoxes::QuantumEraser (QuantumEraser.h:9-62),
 Paradoxes::HardyParadox (HardyParadox.h:11-100), Paradoxes::GeneralElitzurVaidmanBomb
-(GeneralElitzurVaidmanBomb.h:11-125) and Games::CoinFlipping (CoinFlipping.h:11-48).  Each circuit goes to the
-engine as one gate list, and the statistics come from the register's RepeatedMeasure.
+(GeneralElitzurVaidmanBomb.h:11-125), Games::CoinFlipping (CoinFlipping.h:11-48) and Games::MagicSquare
+(MagicSquare.h:9-225).  Each circuit goes to the engine as one gate list, and the statistics come from the
+register's RepeatedMeasure.
 """
 from __future__ import annotations
 
@@ -160,3 +161,78 @@ class CoinFlipping(QuantumAlgorithm):
         ops.append((self.hadamardGate, 0))
         self.ApplyGates(ops)
         return self.Measure()
+
+
+# The players' measurement operators of the quantum strategy for the Mermin-Peres magic-square game
+# (Brassard, Broadbent and Tapp, "Recasting Mermin's multi-player game into the framework of
+# pseudo-telepathy", 2005), as MagicSquare.h:25-90 states them: Alice's for rows 1-3, Bob's for columns 1-3.
+_I = 1j
+_R2 = 1.0 / math.sqrt(2.0)
+_ALICE = (
+    _R2 * np.array([[_I, 0, 0, 1], [0, -_I, 1, 0], [0, _I, 1, 0], [1, 0, 0, _I]]),
+    0.5 * np.array([[_I, 1, 1, _I], [-_I, 1, -1, _I], [_I, 1, -1, -_I], [-_I, 1, 1, -_I]]),
+    0.5 * np.array([[-1, -1, -1, 1], [1, 1, -1, 1], [1, -1, 1, 1], [1, -1, -1, -1]]),
+)
+_BOB = (
+    0.5 * np.array([[_I, -_I, 1, 1], [-_I, -_I, 1, -1], [1, 1, -_I, _I], [-_I, _I, 1, 1]]),
+    0.5 * np.array([[-1, _I, 1, _I], [1, _I, 1, -_I], [1, -_I, 1, _I], [-1, -_I, 1, -_I]]),
+    _R2 * np.array([[1, 0, 0, 1], [-1, 0, 0, 1], [0, 1, 1, 0], [0, 1, -1, 0]]),
+)
+
+
+class MagicSquare(QuantumAlgorithm):
+    """Games::MagicSquare (MagicSquare.h:9-225): Alice (qubits 0, 1) and Bob (qubits 2, 3) share two Bell pairs;
+    given a row a and a column b they apply their strategy operator, measure two bits and complete the third by
+    parity; they win when Alice's bit in column b equals Bob's bit in row a, which the quantum strategy does in
+    every play.  The row, column and who-measures-first choices come from a seeded numpy generator (a
+    clock-seeded std::mt19937_64 in the reference)."""
+
+    def __init__(self, addseed: int = 0, choice_seed: int | None = None, **kw):
+        super().__init__(4, addseed, **kw)
+        self.nrPlays = 100
+        self._rng = np.random.default_rng(choice_seed)
+        self.A = [G.TwoQubitsGate(m) for m in _ALICE]
+        self.B = [G.TwoQubitsGate(m) for m in _BOB]
+        self.h, self.z, self.x, self.cnot = G.HadamardGate(), G.PauliZGate(), G.PauliXGate(), G.CNOTGate()
+        self.setToBasisState(0)
+
+    def getNrPlays(self) -> int:
+        return self.nrPlays
+
+    def setNrPlays(self, n: int) -> None:
+        self.nrPlays = n
+
+    def Execute(self) -> int:
+        wins = 0
+        for _ in range(self.nrPlays):
+            a, b = (int(v) for v in self._rng.integers(1, 4, 2))
+            wins += self.Play(a, b)[0]
+        return wins
+
+    def Play(self, a: int, b: int) -> tuple[bool, int, int]:
+        """(won, Alice's three bits, Bob's three bits) for row a and column b in 1..3 (MagicSquare.h:110-145)"""
+        self.Init()
+        if self._rng.integers(2):
+            ra = self.AliceOperations(a)
+            rb = self.BobOperations(b)
+        else:
+            rb = self.BobOperations(b)
+            ra = self.AliceOperations(a)
+        return ((ra >> (3 - b)) & 1) == ((rb >> (3 - a)) & 1), ra, rb
+
+    def Init(self) -> None:
+        self.setToBasisState(0)
+        self.ApplyGates([(self.h, 0), (self.h, 1), (self.z, 0), (self.z, 1), (self.cnot, 2, 0), (self.cnot, 3, 1),
+                         (self.x, 2), (self.x, 3)])
+
+    def AliceOperations(self, a: int) -> int:
+        if 1 <= a <= 3:
+            self.ApplyGate(self.A[a - 1], 0, 1)
+        r = self.Measure(0, 1) << 1
+        return r | 1 if r in (2, 4) else r
+
+    def BobOperations(self, b: int) -> int:
+        if 1 <= b <= 3:
+            self.ApplyGate(self.B[b - 1], 2, 3)
+        r = self.Measure(2, 3) << 1
+        return r | 1 if r in (0, 6) else r

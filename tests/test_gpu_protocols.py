@@ -385,3 +385,15 @@ def _check_gate_oracles(O):
 def test_gate_built_oracles(Q):
     from qcsim_gb300 import oracles as O
     _check_gate_oracles(O)
+
+
+def test_magic_square(Q):
+    """MagicSquareTests (GamesTests.cpp:28-45): the quantum strategy wins every play"""
+    from qcsim_gb300 import paradoxes as P
+    game = P.MagicSquare(seed=6, choice_seed=7)
+    assert game.Execute() == game.getNrPlays()
+    for a in (1, 2, 3):
+        for b in (1, 2, 3):
+            won, ra, rb = game.Play(a, b)
+            assert won and bin(ra).count("1") % 2 == 0 and bin(rb).count("1") % 2 == 1
+    game.close()

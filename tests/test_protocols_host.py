@@ -270,3 +270,15 @@ def test_n_controlled_gates_with_ancilla():
             assert bits >> (nc + 2) == 0, (nc, c)
             full = c == (1 << nc) - 1
             assert (bits >> nc) & 3 == (3 if full else 0), (nc, c)
+
+
+def test_magic_square(on_oracle):
+    """MagicSquareTests (GamesTests.cpp:28-45): the quantum strategy wins every play"""
+    from qcsim_gb300 import paradoxes as P
+    game = P.MagicSquare(seed=6, choice_seed=7)
+    assert game.Execute() == game.getNrPlays()
+    for a in (1, 2, 3):
+        for b in (1, 2, 3):
+            won, ra, rb = game.Play(a, b)
+            assert won and bin(ra).count("1") % 2 == 0 and bin(rb).count("1") % 2 == 1
+    game.close()
