@@ -17,6 +17,7 @@ Mirrors of QCSim's algorithm classes over the engine, by module:
   distributed        distributed and teleported CNOTs
   paradoxes          quantum eraser, Hardy's paradox, the Elitzur-Vaidman bomb, coin flipping
   oracles            gate-built oracles and the Deutsch-Jozsa, Bernstein-Vazirani and Simon variants on them
+  qml                q-means clustering with swap-test overlaps
   schrodinger        the split-operator Schrodinger simulation
   costmodel          the learned fusion cost model
 """

@@ -282,3 +282,34 @@ def test_magic_square(on_oracle):
             won, ra, rb = game.Play(a, b)
             assert won and bin(ra).count("1") % 2 == 0 and bin(rb).count("1") % 2 == 1
     game.close()
+
+
+def _check_qmeans(make, shots):
+    """QMeansClustering2DTests (QMLTests.cpp:26-120): three clusters of 15 points around (0, 0), (3, 3) and
+    (1.5, 2); clustering converges, and no point measures a larger swap-test overlap with another centroid than
+    with its own (within 4 standard deviations of the shot noise; the reference uses 10^6 shots and no margin)"""
+    from qcsim_gb300 import qml as M
+    rng = np.random.default_rng(15)
+    data = [M.DataPoint(cx + rng.uniform(-1.5, 1.5), cy + rng.uniform(-1.5, 1.5))
+            for cx, cy in ((0.0, 0.0), (3.0, 3.0), (1.5, 2.0)) for _ in range(15)]
+    data = [data[i] for i in rng.permutation(len(data))]
+    qm = make()
+    qm.setData(data)
+    assert qm.Cluster(3, shots)
+    pts, cents = qm.getData(), qm.getCentroids()
+    assert sorted((p.x, p.y) for p in pts) == sorted((p.x, p.y) for p in data)
+    margin = 4 * np.sqrt(shots) / 2
+    for p in pts:
+        qm.SetDataPoint1(p)
+        qm.SetDataPoint2(cents[p.cluster])
+        own = qm.ExecuteWithMultipleMeasurements(shots).get(0, 0)
+        for c, cent in enumerate(cents):
+            if c != p.cluster:
+                qm.SetDataPoint2(cent)
+                assert qm.ExecuteWithMultipleMeasurements(shots).get(0, 0) <= own + margin
+    qm.close()
+
+
+def test_qmeans_clustering(on_oracle):
+    from qcsim_gb300 import qml as M
+    _check_qmeans(lambda: M.QMeansClustering2D(seed=1, choice_seed=2), 4000)
