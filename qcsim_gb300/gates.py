@@ -603,11 +603,36 @@ def to_record(gate: QuantumGate, q0: int, q1: int = 0, q2: int = 0, out=None):
 
 
 def records(gates) -> np.ndarray:
-    """qcs_gate array from (gate, q0, q1, q2) tuples"""
-    arr = np.zeros(len(gates), dtype=L.GATE_DTYPE)
+    """qcs_gate array from (gate, q0, q1, q2) tuples, the same records to_record makes one by one.  Each distinct
+    gate object's matrix, size and traits are read once per call and the columns are filled with whole-array
+    writes, so long lists that reuse a few gate objects (oracle expansions, controlled Grover iterations)
+    convert quickly."""
+    n = len(gates)
+    arr = np.zeros(n, dtype=L.GATE_DTYPE)
+    if n == 0:
+        return arr
+    slot: dict[int, int] = {}
+    sizes, traits, mats = [], [], []
+    inv = np.empty(n, dtype=np.intp)
+    qs = []
     for i, g in enumerate(gates):
-        gate, qs = g[0], list(g[1:]) + [0, 0]
-        to_record(gate, qs[0], qs[1], qs[2], out=arr[i])
+        gate = g[0]
+        j = slot.get(id(gate))
+        if j is None:
+            j = slot[id(gate)] = len(sizes)
+            sizes.append(gate.getQubitsNumber())
+            traits.append(gate.traits())
+            mats.append(np.ascontiguousarray(gate.getRawOperatorMatrix(), dtype=np.complex128).reshape(-1).view(np.float64))
+        inv[i] = j
+        qs.append((tuple(g) + (0, 0, 0))[1:4])
+    q = np.array(qs, dtype=np.uint32)
+    m = np.zeros((len(mats), arr["m"].shape[1]))
+    for j, f in enumerate(mats):
+        m[j, : f.size] = f
+    arr["k"] = np.asarray(sizes, dtype=np.uint32)[inv]
+    arr["traits"] = np.asarray(traits, dtype=np.uint32)[inv]
+    arr["q0"], arr["q1"], arr["q2"] = q[:, 0], q[:, 1], q[:, 2]
+    arr["m"] = m[inv]
     return arr
 
 

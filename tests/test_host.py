@@ -212,3 +212,25 @@ def test_committed_cost_model_is_sane():
     assert np.all(np.isfinite(y)) and y[1] > y[0]
     pm = d["pass_ms"]
     assert all(1.6 < pm[n + 1] / pm[n] < 2.4 for n in range(24, 32))
+
+
+def test_records_match_to_record():
+    """the whole-list conversion gives, byte for byte, the records to_record makes one gate at a time: reused
+    and distinct gate objects, parametrised gates, matrix-only gates of 1-3 qubits, short (gate, q0) tuples"""
+    from qcsim_gb300 import circuits
+    from qcsim_gb300 import gates as G
+    rng = np.random.default_rng(4)
+    h, ccx = G.HadamardGate(), G.ToffoliGate()
+    ops = circuits.layered_circuit(12, 4, seed=9, controlled_frac=0.2)
+    ops += [(h, 3), (ccx, 5, 1, 2), (h, 0), (ccx, 2, 0, 1), (G.RzGate(0.7), 4)]
+    for k in (1, 2, 3):
+        d = 1 << k
+        m = rng.standard_normal((d, d)) + 1j * rng.standard_normal((d, d))
+        ops.append((G.AppliedGate(m, 0, 1, 2), *range(k)))
+    ops = [ops[i] for i in rng.permutation(len(ops))]
+    want = np.zeros(len(ops), dtype=L.GATE_DTYPE)
+    for i, op in enumerate(ops):
+        qs = list(op[1:]) + [0, 0]
+        G.to_record(op[0], qs[0], qs[1], qs[2], out=want[i])
+    assert G.records(ops).tobytes() == want.tobytes()
+    assert G.records([]).size == 0
