@@ -18,6 +18,7 @@ Mirrors of QCSim's algorithm classes over the engine, by module:
   paradoxes          quantum eraser, Hardy's paradox, the Elitzur-Vaidman bomb, coin flipping
   oracles            gate-built oracles and the Deutsch-Jozsa, Bernstein-Vazirani and Simon variants on them
   qml                q-means clustering with swap-test overlaps
+  pauli_simulation   Trotter evolution under a sum of Pauli strings
   schrodinger        the split-operator Schrodinger simulation
   costmodel          the learned fusion cost model
 """

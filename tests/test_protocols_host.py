@@ -313,3 +313,30 @@ def _check_qmeans(make, shots):
 def test_qmeans_clustering(on_oracle):
     from qcsim_gb300 import qml as M
     _check_qmeans(lambda: M.QMeansClustering2D(seed=1, choice_seed=2), 4000)
+
+
+def _check_pauli_simulation(S, cases=10):
+    """PauliSimulationTests (SimulationTests.cpp:21-80): 3 qubits, 1-5 random Pauli-string terms with
+    coefficients -U(0.1, 10), t = 1 / (2 pi) in 100 Trotter steps; fidelity >= 0.999 with exp(-i t H)|0>"""
+    import math
+    rng = np.random.default_rng(21)
+    t = 1.0 / (2.0 * math.pi)
+    for _ in range(cases):
+        sim = S.PauliDecomposedHamiltonianSimulation(3, t, 100, seed=1)
+        sim.setToBasisState(0)
+        term = S.PauliStringSimulation()
+        for _ in range(int(rng.integers(1, 6))):
+            for q in range(3):
+                term.setOperatorForQubit(q, int(rng.integers(0, 3)))
+            sim.AddTerm(-rng.uniform(0.1, 10.0), term)
+        ex = sim.getEvolutionOperator(t) @ sim.getRegisterStorage()
+        sim.setToBasisState(0)
+        sim.Execute()
+        v = sim.getRegisterStorage()
+        assert abs(np.vdot(ex, v)) ** 2 >= 0.999
+        sim.close()
+
+
+def test_pauli_hamiltonian_simulation(on_oracle):
+    from qcsim_gb300 import pauli_simulation as S
+    _check_pauli_simulation(S, cases=4)
