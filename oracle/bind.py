@@ -67,6 +67,7 @@ _REF_SIG = {
     "qr_ising_energy": (_d, [_u32, _u32, _pu32, _pd, _pd, _u64]),
     "qr_uniforms": (None, [_u64, _sz, _pd]),
     "qr_nqubits_gate": (_i, [_h, _u32, _pd, _u32, _u32, _i, _pd]),
+    "qr_pauli_simulation": (_i, [_u32, _pd, _u32, C.c_void_p, _pd, _d, _u32, _pd]),
 }
 
 _oracle = None

@@ -18,6 +18,7 @@
 #include "IsingModel.h"
 #include "NQubitsQuantumGate.h"
 #include "NQubitsControlledQuantumGate.h"
+#include "PauliStringSimulation.h"
 
 #include "qcs_oracle.h"  // gate codes and the qo_gate record layout
 
@@ -275,6 +276,31 @@ int qr_nqubits_gate(void* r, uint32_t n, const double* op, uint32_t k, uint32_t 
 				ext_out[2 * (i * NB + j)] = ext(i, j).real();
 				ext_out[2 * (i * NB + j) + 1] = ext(i, j).imag();
 			}
+	return 0;
+}
+
+// QuantumSimulation::PauliDecomposedHamiltonianSimulation on n qubits from the state in (interleaved) with
+// nterms Pauli strings (ops: nterms x n codes, 0 = Z, 1 = X, 2 = Y) and coefficients, simulation time t in
+// steps Trotter steps; the state after Execute into out
+int qr_pauli_simulation(uint32_t n, const double* in, uint32_t nterms, const uint8_t* ops, const double* coeffs, double t,
+                        uint32_t steps, double* out) {
+	using PauliOp = PauliString::PauliString::PauliOp;
+	QuantumSimulation::PauliDecomposedHamiltonianSimulation<> sim(n, t, steps);
+	const Eigen::Index NB = Eigen::Index(1) << n;
+	Eigen::VectorXcd v(NB);
+	for (Eigen::Index i = 0; i < NB; ++i) v(i) = std::complex<double>(in[2 * i], in[2 * i + 1]);
+	sim.setRegisterStorage(v);
+	for (uint32_t k = 0; k < nterms; ++k) {
+		QuantumSimulation::PauliStringSimulation<> term(0., n);
+		for (uint32_t q = 0; q < n; ++q) term.setOperatorForQubit(q, static_cast<PauliOp>(ops[k * n + q]));
+		sim.AddTerm(coeffs[k], term);
+	}
+	sim.Execute();
+	const Eigen::VectorXcd& s = sim.getRegisterStorage();
+	for (Eigen::Index i = 0; i < NB; ++i) {
+		out[2 * i] = s(i).real();
+		out[2 * i + 1] = s(i).imag();
+	}
 	return 0;
 }
 

@@ -340,3 +340,26 @@ def _check_pauli_simulation(S, cases=10):
 def test_pauli_hamiltonian_simulation(on_oracle):
     from qcsim_gb300 import pauli_simulation as S
     _check_pauli_simulation(S, cases=4)
+
+
+def _check_pauli_golden(S, tol):
+    """the mirror's Trotter evolution against QCSim's own PauliDecomposedHamiltonianSimulation::Execute on the
+    same inputs (tests/golden/pauli.npz, made by tests/golden/make_pauli.py from the compiled reference)"""
+    from pathlib import Path
+    g = np.load(Path(__file__).resolve().parent / "golden" / "pauli.npz")
+    for i, (n, nt) in enumerate(g["cases"]):
+        sim = S.PauliDecomposedHamiltonianSimulation(int(n), float(g["times"][i]), int(g["steps"][i]), seed=1)
+        sim.setRegisterStorage(g[f"psi{i}"])
+        for ops, c in zip(g[f"ops{i}"], g[f"coeffs{i}"]):
+            term = S.PauliStringSimulation(0.0, int(n))
+            for q, op in enumerate(ops):
+                term.setOperatorForQubit(q, int(op))
+            sim.AddTerm(float(c), term)
+        sim.Execute()
+        assert np.abs(sim.getRegisterStorage() - g[f"out{i}"]).max() <= tol, i
+        sim.close()
+
+
+def test_pauli_simulation_matches_reference(on_oracle):
+    from qcsim_gb300 import pauli_simulation as S
+    _check_pauli_golden(S, 1e-12)
