@@ -19,6 +19,7 @@
 #include "NQubitsQuantumGate.h"
 #include "NQubitsControlledQuantumGate.h"
 #include "PauliStringSimulation.h"
+#include "Oracle.h"
 
 #include "qcs_oracle.h"  // gate codes and the qo_gate record layout
 
@@ -105,6 +106,16 @@ unsigned traits_of(const QC::Gates::QuantumGate<>& g) {
 	if (g.isControlQubit(1)) t |= QO_TR_CONTROLQ1;
 	return t;
 }
+
+// function objects for the gate-built oracles: a table of values over the oracle's input qubits
+struct TableFunction {
+	std::vector<size_t> values;
+	size_t operator()(size_t state) const { return values[state]; }
+};
+struct BoolTableFunction {
+	std::vector<size_t> values;
+	bool operator()(size_t state) const { return values[state] != 0; }
+};
 
 }  // namespace
 
@@ -300,6 +311,36 @@ int qr_pauli_simulation(uint32_t n, const double* in, uint32_t nterms, const uin
 	for (Eigen::Index i = 0; i < NB; ++i) {
 		out[2 * i] = s(i).real();
 		out[2 * i + 1] = s(i).imag();
+	}
+	return 0;
+}
+
+// QC::Oracles::OracleWithGatesSimpleFunction (simple != 0; f(x) != 0 flips the target) or OracleWithGates (f(x) xored
+// into the qubits from target up) over the input qubits [start, end] with ancillas from anc, f given as a table of
+// 2^(end - start + 1) values; Execute on the n-qubit state inout (interleaved), in place
+int qr_oracle_with_gates(uint32_t n, uint32_t start, uint32_t end, uint32_t target, uint32_t anc, int simple,
+                         const uint64_t* table, double* inout) {
+	SeededRegister reg(n);
+	const Eigen::Index NB = Eigen::Index(1) << n;
+	Eigen::VectorXcd v(NB);
+	for (Eigen::Index i = 0; i < NB; ++i) v(i) = std::complex<double>(inout[2 * i], inout[2 * i + 1]);
+	reg.setRegisterStorage(v);
+	const size_t nv = size_t(1) << (end - start + 1);
+	if (simple) {
+		BoolTableFunction f{std::vector<size_t>(table, table + nv)};
+		QC::Oracles::OracleWithGatesSimpleFunction<BoolTableFunction> oracle(n, start, end, target, anc);
+		oracle.setFunction(f);
+		oracle.Execute(reg);
+	} else {
+		TableFunction f{std::vector<size_t>(table, table + nv)};
+		QC::Oracles::OracleWithGates<TableFunction> oracle(n, start, end, target, anc);
+		oracle.setFunction(f);
+		oracle.Execute(reg);
+	}
+	const Eigen::VectorXcd& s = reg.getRegisterStorage();
+	for (Eigen::Index i = 0; i < NB; ++i) {
+		inout[2 * i] = s(i).real();
+		inout[2 * i + 1] = s(i).imag();
 	}
 	return 0;
 }

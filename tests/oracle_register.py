@@ -82,6 +82,20 @@ class OracleBackedRegister:
         if qubit is None:
             qubit, c1, c2 = gate.getQubit1(), gate.getQubit2(), gate.getQubit3()
         self.r.apply([self._oracle_op(gate, qubit, c1, c2)])
+        if self._recording:
+            self._recorded.append((gate.getRawOperatorMatrix().copy(), qubit, c1, c2))
+
+    # record / replay as the register's ComputeStart / ComputeEnd / Uncompute (QubitRegister.h:536-590)
+    _recording = False
+
+    def ComputeStart(self):
+        self._recording, self._recorded = True, []
+
+    def ComputeEnd(self):
+        self._recording = False
+
+    def Uncompute(self):
+        self.r.apply([(G.AppliedGate(m.conj().T, q0, q1, q2), q0, q1, q2) for m, q0, q1, q2 in reversed(self._recorded)])
 
     def ApplyGates(self, ops):
         ops = getattr(ops, "ops", ops)  # a gates.PreparedGates carries its tuples

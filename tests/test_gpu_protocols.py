@@ -478,3 +478,26 @@ def _check_pauli_golden(S, tol):
 def test_pauli_simulation_matches_reference(Q):
     from qcsim_gb300 import pauli_simulation as S
     _check_pauli_golden(S, 1e-12)
+
+
+def _check_oracles_golden(O, make_reg, tol):
+    """the mirror's gate-built oracles against QCSim's own OracleWithGates / OracleWithGatesSimpleFunction
+    Execute on the same states and function tables (tests/golden/oracles.npz, made by tests/golden/make_oracles.py
+    from the compiled reference)"""
+    from pathlib import Path
+    g = np.load(Path(__file__).resolve().parent / "golden" / "oracles.npz")
+    for i, (n, start, end, target, anc, simple) in enumerate(g["cases"].tolist()):
+        values = g[f"table{i}"].tolist()
+        cls = O.OracleWithGatesSimpleFunction if simple else O.OracleWithGates
+        oracle = cls(n, start, end, target, anc)
+        oracle.setFunction(lambda x, v=values: v[x])
+        reg = make_reg(n)
+        reg.setRegisterStorage(g[f"psi{i}"])
+        oracle.Execute(reg)
+        assert np.abs(reg.getRegisterStorage() - g[f"out{i}"]).max() <= tol, i
+        reg.close()
+
+
+def test_gate_built_oracles_match_reference(Q):
+    from qcsim_gb300 import oracles as O
+    _check_oracles_golden(O, lambda n: Q.QubitRegister(n, seed=1), 1e-12)
