@@ -69,6 +69,9 @@ _REF_SIG = {
     "qr_nqubits_gate": (_i, [_h, _u32, _pd, _u32, _u32, _i, _pd]),
     "qr_pauli_simulation": (_i, [_u32, _pd, _u32, C.c_void_p, _pd, _d, _u32, _pd]),
     "qr_oracle_with_gates": (_i, [_u32, _u32, _u32, _u32, _u32, _i, C.c_void_p, _pd]),
+    "qr_grover": (_i, [_u32, _u64, _pd]),
+    "qr_draper": (_i, [_u32, _i, _pd, _pd]),
+    "qr_phase_estimation": (_i, [_pd, _u32, _u32, _u32, _pd, _pd]),
 }
 
 _oracle = None

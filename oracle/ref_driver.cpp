@@ -21,6 +21,18 @@
 #include "PauliStringSimulation.h"
 #include "Oracle.h"
 
+// GroverAlgorithm.h asserts unitarity with the name of QCSim's test-suite helper; this is the driver's own version
+bool checkUnitary(const Eigen::MatrixXcd& m) {
+	const Eigen::MatrixXcd r = m.adjoint() * m;
+	for (Eigen::Index i = 0; i < r.rows(); ++i)
+		for (Eigen::Index j = 0; j < r.cols(); ++j)
+			if (std::abs(r(i, j) - std::complex<double>(i == j ? 1. : 0., 0.)) > 1e-10) return false;
+	return true;
+}
+#include "GroverAlgorithm.h"
+#include "DraperAdder.h"
+#include "PhaseEstimation.h"
+
 #include "qcs_oracle.h"  // gate codes and the qo_gate record layout
 
 namespace {
@@ -105,6 +117,34 @@ unsigned traits_of(const QC::Gates::QuantumGate<>& g) {
 	if (g.isControlled()) t |= QO_TR_CONTROLLED;
 	if (g.isControlQubit(1)) t |= QO_TR_CONTROLQ1;
 	return t;
+}
+
+// the algorithms' protected ExecuteWithoutMeasurement exposed
+class GroverProbe : public Grover::GroverAlgorithm<> {
+public:
+	using Grover::GroverAlgorithm<>::GroverAlgorithm;
+	void Run() { ExecuteWithoutMeasurement(); }
+};
+template <class Adder> class AdderProbe : public Adder {
+public:
+	using Adder::Adder;
+	void Run() { this->ExecuteWithoutMeasurement(); }
+};
+class PhaseEstimationProbe : public QC::SubAlgo::PhaseEstimation<> {
+public:
+	using QC::SubAlgo::PhaseEstimation<>::PhaseEstimation;
+	void Run(Reg& r) { ExecuteWithoutMeasurement(r); }
+};
+
+void to_vector(const double* in, Eigen::Index nb, Eigen::VectorXcd& v) {
+	v.resize(nb);
+	for (Eigen::Index i = 0; i < nb; ++i) v(i) = std::complex<double>(in[2 * i], in[2 * i + 1]);
+}
+void from_vector(const Eigen::VectorXcd& v, double* out) {
+	for (Eigen::Index i = 0; i < v.size(); ++i) {
+		out[2 * i] = v(i).real();
+		out[2 * i + 1] = v(i).imag();
+	}
 }
 
 // function objects for the gate-built oracles: a table of values over the oracle's input qubits
@@ -342,6 +382,52 @@ int qr_oracle_with_gates(uint32_t n, uint32_t start, uint32_t end, uint32_t targ
 		inout[2 * i] = s(i).real();
 		inout[2 * i + 1] = s(i).imag();
 	}
+	return 0;
+}
+
+// Grover::GroverAlgorithm on n qubits with the marked state: the state after ExecuteWithoutMeasurement into out
+int qr_grover(uint32_t n, uint64_t marked, double* out) {
+	GroverProbe g(n);
+	g.setCorrectQuestionState(marked);
+	g.Run();
+	from_vector(g.getRegisterStorage(), out);
+	return 0;
+}
+
+// Adders::DraperAdder (carry == 0, 2N qubits) or DraperAdderWithCarry (2N + 1 qubits) from the state in: the state
+// after ExecuteWithoutMeasurement into out
+int qr_draper(uint32_t N, int carry, const double* in, double* out) {
+	Eigen::VectorXcd v;
+	if (carry) {
+		AdderProbe<Adders::DraperAdderWithCarry<>> a(N);
+		to_vector(in, a.getNrBasisStates(), v);
+		a.setRegisterStorage(v);
+		a.Run();
+		from_vector(a.getRegisterStorage(), out);
+	} else {
+		AdderProbe<Adders::DraperAdder<>> a(N);
+		to_vector(in, a.getNrBasisStates(), v);
+		a.setRegisterStorage(v);
+		a.Run();
+		from_vector(a.getRegisterStorage(), out);
+	}
+	return 0;
+}
+
+// QC::SubAlgo::PhaseEstimation of the 2^k x 2^k operator op (row-major interleaved) on an N-qubit register with L
+// precision qubits, starting from the state in: the state after ExecuteWithoutMeasurement into out
+int qr_phase_estimation(const double* op, uint32_t k, uint32_t N, uint32_t L, const double* in, double* out) {
+	const Eigen::Index D = Eigen::Index(1) << k;
+	Mat U(D, D);
+	for (Eigen::Index i = 0; i < D; ++i)
+		for (Eigen::Index j = 0; j < D; ++j) U(i, j) = std::complex<double>(op[2 * (i * D + j)], op[2 * (i * D + j) + 1]);
+	PhaseEstimationProbe pe(U, N, L);
+	SeededRegister reg(N);
+	Eigen::VectorXcd v;
+	to_vector(in, reg.getNrBasisStates(), v);
+	reg.setRegisterStorage(v);
+	pe.Run(reg);
+	from_vector(reg.getRegisterStorage(), out);
 	return 0;
 }
 

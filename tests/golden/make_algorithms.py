@@ -1,0 +1,68 @@
+"""Generate tests/golden/algorithms.npz from QCSim's own Grover search, Draper adders and phase estimation (the
+compiled reference).
+
+Run in a checkout that has the QCSim sources (oracle/Makefile target `ref` builds oracle/_ref/libqcsref.so from them):
+
+    make -C oracle ref && python tests/golden/make_algorithms.py
+
+Each case is the state after the class's ExecuteWithoutMeasurement (GroverAlgorithm.h:89-98, DraperAdder.h:38-57 and
+:88-112, PhaseEstimation.h:195-215): Grover from its equal superposition with the given marked state; the adders from
+a random normalised superposition of inputs; phase estimation of a random unitary on the function register.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import sys
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parents[2]
+sys.path.insert(0, str(ROOT))
+
+from oracle import bind as B  # noqa: E402
+
+OUT = Path(__file__).resolve().parent / "algorithms.npz"
+
+GROVER = [(3, 5), (5, 17), (7, 100), (9, 300)]  # (qubits, marked state)
+DRAPER = [(2, 0), (3, 0), (4, 0), (2, 1), (3, 1), (4, 1)]  # (N, with carry)
+PHASE = [(1, 4, 3), (2, 7, 5), (3, 8, 5)]  # (operator qubits k, register qubits N, precision qubits L), k = N - L
+
+
+def pd(a: np.ndarray):
+    return a.view(np.float64).ctypes.data_as(C.POINTER(C.c_double))
+
+
+def unit(rng, n: int) -> np.ndarray:
+    v = rng.standard_normal(1 << n) + 1j * rng.standard_normal(1 << n)
+    return np.ascontiguousarray(v / np.linalg.norm(v))
+
+
+def main() -> None:
+    lib = B.ref()
+    rng = np.random.default_rng(20261207)
+    out = {"grover": np.array(GROVER, dtype=np.int64), "draper": np.array(DRAPER, dtype=np.int64),
+           "phase": np.array(PHASE, dtype=np.int64)}
+    for i, (n, marked) in enumerate(GROVER):
+        res = np.zeros(1 << n, dtype=np.complex128)
+        assert lib.qr_grover(n, marked, pd(res)) == 0
+        out[f"grover{i}"] = res
+    for i, (N, carry) in enumerate(DRAPER):
+        psi = unit(rng, 2 * N + carry)
+        res = np.zeros_like(psi)
+        assert lib.qr_draper(N, carry, pd(psi), pd(res)) == 0
+        out[f"draper_in{i}"], out[f"draper{i}"] = psi, res
+    for i, (k, N, L) in enumerate(PHASE):
+        d = 1 << k
+        u, _ = np.linalg.qr(rng.standard_normal((d, d)) + 1j * rng.standard_normal((d, d)))
+        u = np.ascontiguousarray(u)
+        psi = unit(rng, N)
+        res = np.zeros_like(psi)
+        assert lib.qr_phase_estimation(pd(u), k, N, L, pd(psi), pd(res)) == 0
+        out[f"phase_u{i}"], out[f"phase_in{i}"], out[f"phase{i}"] = u, psi, res
+    np.savez_compressed(OUT, **out)
+    print("wrote", OUT, OUT.stat().st_size, "bytes")
+
+
+if __name__ == "__main__":
+    main()

@@ -386,3 +386,33 @@ def _check_oracles_golden(O, make_reg, tol):
 def test_gate_built_oracles_match_reference():
     from qcsim_gb300 import oracles as O
     _check_oracles_golden(O, lambda n: OracleBackedRegister(n, seed=1), 1e-12)
+
+
+def _check_algorithms_golden(A, make_reg, tol):
+    """the mirrors' pre-measurement states against QCSim's own Grover search, Draper adders and phase estimation
+    (tests/golden/algorithms.npz, made by tests/golden/make_algorithms.py from the compiled reference)"""
+    from pathlib import Path
+    g = np.load(Path(__file__).resolve().parent / "golden" / "algorithms.npz")
+    for i, (n, marked) in enumerate(g["grover"].tolist()):
+        gr = A.GroverAlgorithm(n, seed=1)
+        gr.setCorrectQuestionState(marked)
+        gr.ExecuteWithoutMeasurement()
+        assert np.abs(gr.getRegisterStorage() - g[f"grover{i}"]).max() <= tol, ("grover", i)
+        gr.close()
+    for i, (N, carry) in enumerate(g["draper"].tolist()):
+        ad = (A.DraperAdderWithCarry if carry else A.DraperAdder)(N, seed=1)
+        ad.setRegisterStorage(g[f"draper_in{i}"])
+        ad.ExecuteWithoutMeasurement()
+        assert np.abs(ad.getRegisterStorage() - g[f"draper{i}"]).max() <= tol, ("draper", i)
+        ad.close()
+    for i, (k, N, L) in enumerate(g["phase"].tolist()):
+        pe = A.PhaseEstimation(g[f"phase_u{i}"], N, L)
+        reg = make_reg(N)
+        reg.setRegisterStorage(g[f"phase_in{i}"])
+        pe.ExecuteWithoutMeasurement(reg)
+        assert np.abs(reg.getRegisterStorage() - g[f"phase{i}"]).max() <= tol, ("phase", i)
+        reg.close()
+
+
+def test_algorithms_match_reference(on_oracle):
+    _check_algorithms_golden(A, lambda n: OracleBackedRegister(n, seed=1), 1e-12)
