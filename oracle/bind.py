@@ -72,6 +72,7 @@ _REF_SIG = {
     "qr_grover": (_i, [_u32, _u64, _pd]),
     "qr_draper": (_i, [_u32, _i, _pd, _pd]),
     "qr_phase_estimation": (_i, [_pd, _u32, _u32, _u32, _pd, _pd]),
+    "qr_vqe_term": (_i, [_u32, C.c_void_p, _u32, _pd, _pd]),
 }
 
 _oracle = None

@@ -32,6 +32,7 @@ bool checkUnitary(const Eigen::MatrixXcd& m) {
 #include "GroverAlgorithm.h"
 #include "DraperAdder.h"
 #include "PhaseEstimation.h"
+#include "VQE.h"
 
 #include "qcs_oracle.h"  // gate codes and the qo_gate record layout
 
@@ -427,6 +428,20 @@ int qr_phase_estimation(const double* op, uint32_t k, uint32_t N, uint32_t L, co
 	to_vector(in, reg.getNrBasisStates(), v);
 	reg.setRegisterStorage(v);
 	pe.Run(reg);
+	from_vector(reg.getRegisterStorage(), out);
+	return 0;
+}
+
+// VQE::PauliStringVQE on n qubits with the operator codes ops (0 = Z, 1 = X, 2 = Y): from |0>, Ansatz with the
+// parameters, then Execute (the rotation into the measured basis); the state into out
+int qr_vqe_term(uint32_t n, const uint8_t* ops, uint32_t nparams, const double* params, double* out) {
+	using PauliOp = PauliString::PauliString::PauliOp;
+	VQE::PauliStringVQE<> term(static_cast<int>(n));
+	for (uint32_t q = 0; q < n; ++q) term.setOperatorForQubit(q, static_cast<PauliOp>(ops[q]));
+	SeededRegister reg(n);
+	reg.setToBasisState(0);
+	term.Ansatz(reg, std::vector<double>(params, params + nparams));
+	term.Execute(reg);
 	from_vector(reg.getRegisterStorage(), out);
 	return 0;
 }

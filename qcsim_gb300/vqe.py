@@ -11,19 +11,25 @@ from .algorithms import QuantumAlgorithm
 
 
 class PauliStringVQE:
-    """VQE::PauliStringVQE (VQE.h:21-150): one Pauli string (an operator 'I', 'X', 'Y' or 'Z' per qubit) with a
-    coefficient"""
+    """VQE::PauliStringVQE (VQE.h:21-150): one Pauli string (an operator 'X', 'Y' or 'Z' per qubit, Z by default as
+    in the reference's PauliString, PauliString.h:15) with a coefficient.  The reference's energy estimate takes the
+    parity of every qubit, so a qubit left at Z (or given 'I', accepted as a synonym here) enters it as Z."""
+
+    _CODES = {0: "Z", 1: "X", 2: "Y"}  # PauliString::PauliOp (PauliString.h:8-13)
 
     def __init__(self, nrQubits: int):
-        self.ops = ["I"] * nrQubits
+        self.ops = ["Z"] * nrQubits
         self.coefficient = 1.0
         self.rx, self.ry = G.RxGate(0.5 * math.pi), G.RyGate(-0.5 * math.pi)
         self.cnot = G.CNOTGate()
 
-    def setOperatorForQubit(self, qubit: int, op: str) -> None:
+    def setOperatorForQubit(self, qubit: int, op) -> None:
+        """op: 'X', 'Y', 'Z' (or 'I', the same as Z here), or the reference's PauliOp code 0 = Z, 1 = X, 2 = Y"""
+        op = self._CODES.get(op, op) if isinstance(op, int) else op
         if op not in ("I", "X", "Y", "Z"):
-            raise ValueError("Pauli operator must be I, X, Y or Z")
-        self.ops[qubit] = op
+            raise ValueError("Pauli operator must be X, Y or Z (or I)")
+        if qubit < len(self.ops):
+            self.ops[qubit] = op
 
     def getOperatorForQubit(self, qubit: int) -> str:
         return self.ops[qubit]
@@ -37,7 +43,7 @@ class PauliStringVQE:
     def Execute(self, reg) -> int:
         """rotate each qubit into the measured operator's eigenbasis (VQE.h:33-44)"""
         for q in range(reg.getNrQubits()):
-            op = self.getOperatorForQubit(q) if q < len(self.ops) else "I"
+            op = self.getOperatorForQubit(q) if q < len(self.ops) else "Z"
             if op == "X":
                 reg.ApplyGate(self.ry, q)
             elif op == "Y":

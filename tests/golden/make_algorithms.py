@@ -7,7 +7,8 @@ Run in a checkout that has the QCSim sources (oracle/Makefile target `ref` build
 
 Each case is the state after the class's ExecuteWithoutMeasurement (GroverAlgorithm.h:89-98, DraperAdder.h:38-57 and
 :88-112, PhaseEstimation.h:195-215): Grover from its equal superposition with the given marked state; the adders from
-a random normalised superposition of inputs; phase estimation of a random unitary on the function register.
+a random normalised superposition of inputs; phase estimation of a random unitary on the function register; and
+VQE's PauliStringVQE Ansatz followed by Execute (VQE.h:33-114) from |0> with random parameters and operators.
 """
 from __future__ import annotations
 
@@ -27,6 +28,7 @@ OUT = Path(__file__).resolve().parent / "algorithms.npz"
 GROVER = [(3, 5), (5, 17), (7, 100), (9, 300)]  # (qubits, marked state)
 DRAPER = [(2, 0), (3, 0), (4, 0), (2, 1), (3, 1), (4, 1)]  # (N, with carry)
 PHASE = [(1, 4, 3), (2, 7, 5), (3, 8, 5)]  # (operator qubits k, register qubits N, precision qubits L), k = N - L
+VQE = [(1, 2), (2, 4), (3, 9), (4, 14), (5, 30)]  # (qubits, parameters): the ansatz's single layer and CNOT-ring layers
 
 
 def pd(a: np.ndarray):
@@ -42,7 +44,7 @@ def main() -> None:
     lib = B.ref()
     rng = np.random.default_rng(20261207)
     out = {"grover": np.array(GROVER, dtype=np.int64), "draper": np.array(DRAPER, dtype=np.int64),
-           "phase": np.array(PHASE, dtype=np.int64)}
+           "phase": np.array(PHASE, dtype=np.int64), "vqe": np.array(VQE, dtype=np.int64)}
     for i, (n, marked) in enumerate(GROVER):
         res = np.zeros(1 << n, dtype=np.complex128)
         assert lib.qr_grover(n, marked, pd(res)) == 0
@@ -60,6 +62,13 @@ def main() -> None:
         res = np.zeros_like(psi)
         assert lib.qr_phase_estimation(pd(u), k, N, L, pd(psi), pd(res)) == 0
         out[f"phase_u{i}"], out[f"phase_in{i}"], out[f"phase{i}"] = u, psi, res
+    for i, (n, npar) in enumerate(VQE):
+        ops = np.ascontiguousarray(rng.integers(0, 3, n).astype(np.uint8))
+        params = np.ascontiguousarray(rng.uniform(-np.pi, np.pi, npar))
+        res = np.zeros(1 << n, dtype=np.complex128)
+        assert lib.qr_vqe_term(n, ops.ctypes.data_as(C.c_void_p), npar, params.ctypes.data_as(C.POINTER(C.c_double)),
+                               pd(res)) == 0
+        out[f"vqe_ops{i}"], out[f"vqe_params{i}"], out[f"vqe{i}"] = ops, params, res
     np.savez_compressed(OUT, **out)
     print("wrote", OUT, OUT.stat().st_size, "bytes")
 

@@ -504,7 +504,8 @@ def test_gate_built_oracles_match_reference(Q):
 
 
 def _check_algorithms_golden(A, make_reg, tol):
-    """the mirrors' pre-measurement states against QCSim's own Grover search, Draper adders and phase estimation
+    """the mirrors' pre-measurement states against QCSim's own Grover search, Draper adders, phase estimation and
+    VQE ansatz
     (tests/golden/algorithms.npz, made by tests/golden/make_algorithms.py from the compiled reference)"""
     from pathlib import Path
     g = np.load(Path(__file__).resolve().parent / "golden" / "algorithms.npz")
@@ -526,6 +527,17 @@ def _check_algorithms_golden(A, make_reg, tol):
         reg.setRegisterStorage(g[f"phase_in{i}"])
         pe.ExecuteWithoutMeasurement(reg)
         assert np.abs(reg.getRegisterStorage() - g[f"phase{i}"]).max() <= tol, ("phase", i)
+        reg.close()
+    from qcsim_gb300 import vqe as V
+    for i, (n, npar) in enumerate(g["vqe"].tolist()):
+        term = V.PauliStringVQE(n)
+        for q, op in enumerate(g[f"vqe_ops{i}"].tolist()):
+            term.setOperatorForQubit(q, int(op))
+        reg = make_reg(n)
+        reg.setToBasisState(0)
+        term.Ansatz(reg, g[f"vqe_params{i}"].tolist())
+        term.Execute(reg)
+        assert np.abs(reg.getRegisterStorage() - g[f"vqe{i}"]).max() <= tol, ("vqe", i)
         reg.close()
 
 
