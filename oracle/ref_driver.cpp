@@ -33,6 +33,7 @@ bool checkUnitary(const Eigen::MatrixXcd& m) {
 #include "DraperAdder.h"
 #include "PhaseEstimation.h"
 #include "VQE.h"
+#include "ShorAlgorithm.h"
 
 #include "qcs_oracle.h"  // gate codes and the qo_gate record layout
 
@@ -130,6 +131,11 @@ template <class Adder> class AdderProbe : public Adder {
 public:
 	using Adder::Adder;
 	void Run() { this->ExecuteWithoutMeasurement(); }
+};
+class ShorPhaseEstimationProbe : public QC::SubAlgo::ShorPhaseEstimation<> {
+public:
+	using QC::SubAlgo::ShorPhaseEstimation<>::ShorPhaseEstimation;
+	void Run(Reg& r) { ExecuteWithoutMeasurement(r); }
 };
 class PhaseEstimationProbe : public QC::SubAlgo::PhaseEstimation<> {
 public:
@@ -442,6 +448,18 @@ int qr_vqe_term(uint32_t n, const uint8_t* ops, uint32_t nparams, const double* 
 	reg.setToBasisState(0);
 	term.Ansatz(reg, std::vector<double>(params, params + nparams));
 	term.Execute(reg);
+	from_vector(reg.getRegisterStorage(), out);
+	return 0;
+}
+
+// Shor's period finding: QC::SubAlgo::ShorPhaseEstimation of Shor::Fx (number C, base a) on N qubits with L x qubits;
+// the state after ExecuteWithoutMeasurement into out
+int qr_shor_period_finding(uint32_t C, uint32_t a, uint32_t N, uint32_t L, double* out) {
+	Shor::Fx<> f(L, N - L, C);
+	f.setParam(a);
+	ShorPhaseEstimationProbe pe(f, N, L);
+	SeededRegister reg(N);
+	pe.Run(reg);
 	from_vector(reg.getRegisterStorage(), out);
 	return 0;
 }

@@ -7,8 +7,9 @@ Run in a checkout that has the QCSim sources (oracle/Makefile target `ref` build
 
 Each case is the state after the class's ExecuteWithoutMeasurement (GroverAlgorithm.h:89-98, DraperAdder.h:38-57 and
 :88-112, PhaseEstimation.h:195-215): Grover from its equal superposition with the given marked state; the adders from
-a random normalised superposition of inputs; phase estimation of a random unitary on the function register; and
-VQE's PauliStringVQE Ansatz followed by Execute (VQE.h:33-114) from |0> with random parameters and operators.
+a random normalised superposition of inputs; phase estimation of a random unitary on the function register; VQE's
+PauliStringVQE Ansatz followed by Execute (VQE.h:33-114) from |0> with random parameters and operators; and Shor's
+period finding, ShorPhaseEstimation of Shor::Fx (PhaseEstimation.h:100-149, ShorAlgorithm.h:54-104).
 """
 from __future__ import annotations
 
@@ -29,6 +30,9 @@ GROVER = [(3, 5), (5, 17), (7, 100), (9, 300)]  # (qubits, marked state)
 DRAPER = [(2, 0), (3, 0), (4, 0), (2, 1), (3, 1), (4, 1)]  # (N, with carry)
 PHASE = [(1, 4, 3), (2, 7, 5), (3, 8, 5)]  # (operator qubits k, register qubits N, precision qubits L), k = N - L
 VQE = [(1, 2), (2, 4), (3, 9), (4, 14), (5, 30)]  # (qubits, parameters): the ansatz's single layer and CNOT-ring layers
+# (C, a, register qubits N, x qubits L); a^(2^(L-1)) must fit in 64 bits, since Fx squares in 64-bit arithmetic and
+# asserts that each modular multiplier is unitary (ShorAlgorithm.h:62-101)
+SHOR = [(15, 7, 7, 3), (15, 2, 7, 3), (15, 11, 7, 3), (21, 2, 11, 6)]
 
 
 def pd(a: np.ndarray):
@@ -44,7 +48,8 @@ def main() -> None:
     lib = B.ref()
     rng = np.random.default_rng(20261207)
     out = {"grover": np.array(GROVER, dtype=np.int64), "draper": np.array(DRAPER, dtype=np.int64),
-           "phase": np.array(PHASE, dtype=np.int64), "vqe": np.array(VQE, dtype=np.int64)}
+           "phase": np.array(PHASE, dtype=np.int64), "vqe": np.array(VQE, dtype=np.int64),
+           "shor": np.array(SHOR, dtype=np.int64)}
     for i, (n, marked) in enumerate(GROVER):
         res = np.zeros(1 << n, dtype=np.complex128)
         assert lib.qr_grover(n, marked, pd(res)) == 0
@@ -69,6 +74,10 @@ def main() -> None:
         assert lib.qr_vqe_term(n, ops.ctypes.data_as(C.c_void_p), npar, params.ctypes.data_as(C.POINTER(C.c_double)),
                                pd(res)) == 0
         out[f"vqe_ops{i}"], out[f"vqe_params{i}"], out[f"vqe{i}"] = ops, params, res
+    for i, (c, a, n, L) in enumerate(SHOR):
+        res = np.zeros(1 << n, dtype=np.complex128)
+        assert lib.qr_shor_period_finding(c, a, n, L, pd(res)) == 0
+        out[f"shor{i}"] = res
     np.savez_compressed(OUT, **out)
     print("wrote", OUT, OUT.stat().st_size, "bytes")
 

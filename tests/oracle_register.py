@@ -104,6 +104,10 @@ class OracleBackedRegister:
         if ops:
             self.r.apply(ops)
 
+    def ApplyOperatorOnQubits(self, m, qubits, controls=()):
+        from oracle import nqubits
+        self._set(nqubits.apply_on_qubits(self.r.state(), np.asarray(m, dtype=np.complex128), list(qubits), list(controls)))
+
     def ApplyOperatorMatrix(self, m):
         self._set(np.asarray(m, dtype=np.complex128) @ self.r.state())
 

@@ -389,8 +389,8 @@ def test_gate_built_oracles_match_reference():
 
 
 def _check_algorithms_golden(A, make_reg, tol):
-    """the mirrors' pre-measurement states against QCSim's own Grover search, Draper adders, phase estimation and
-    VQE ansatz
+    """the mirrors' pre-measurement states against QCSim's own Grover search, Draper adders, phase estimation,
+    VQE ansatz and Shor's period finding
     (tests/golden/algorithms.npz, made by tests/golden/make_algorithms.py from the compiled reference)"""
     from pathlib import Path
     g = np.load(Path(__file__).resolve().parent / "golden" / "algorithms.npz")
@@ -423,6 +423,13 @@ def _check_algorithms_golden(A, make_reg, tol):
         term.Ansatz(reg, g[f"vqe_params{i}"].tolist())
         term.Execute(reg)
         assert np.abs(reg.getRegisterStorage() - g[f"vqe{i}"]).max() <= tol, ("vqe", i)
+        reg.close()
+    for i, (c, a, n, L) in enumerate(g["shor"].tolist()):
+        fx = A.Fx(L, n - L, c)
+        fx.setParam(a)
+        reg = make_reg(n)
+        A.ShorPhaseEstimation(fx, n, L).ExecuteWithoutMeasurement(reg)
+        assert np.abs(reg.getRegisterStorage() - g[f"shor{i}"]).max() <= tol, ("shor", i)
         reg.close()
 
 
