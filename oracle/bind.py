@@ -74,6 +74,7 @@ _REF_SIG = {
     "qr_phase_estimation": (_i, [_pd, _u32, _u32, _u32, _pd, _pd]),
     "qr_vqe_term": (_i, [_u32, C.c_void_p, _u32, _pd, _pd]),
     "qr_shor_period_finding": (_i, [_u32, _u32, _u32, _u32, _pd]),
+    "qr_counting": (_i, [_u32, _u32, _u32, C.c_void_p, _pd]),
 }
 
 _oracle = None

@@ -34,6 +34,7 @@ bool checkUnitary(const Eigen::MatrixXcd& m) {
 #include "PhaseEstimation.h"
 #include "VQE.h"
 #include "ShorAlgorithm.h"
+#include "QuantumCountingAlgorithm.h"
 
 #include "qcs_oracle.h"  // gate codes and the qo_gate record layout
 
@@ -461,6 +462,18 @@ int qr_shor_period_finding(uint32_t C, uint32_t a, uint32_t N, uint32_t L, doubl
 	SeededRegister reg(N);
 	pe.Run(reg);
 	from_vector(reg.getRegisterStorage(), out);
+	return 0;
+}
+
+// QuantumCounting::QuantumCountingAlgorithm with P precision and G Grover qubits and the marked states: its
+// (private) ExecuteWithoutMeasurement runs inside ExecuteWithMultipleMeasurements, whose sampling does not collapse,
+// so the register then holds the pre-measurement state, copied into out
+int qr_counting(uint32_t P, uint32_t G, uint32_t nmarked, const uint64_t* marked, double* out) {
+	QuantumCounting::QuantumCountingAlgorithm<> qc(P, G);
+	std::vector<size_t> m(marked, marked + nmarked);
+	qc.SetMarkedStates(m);
+	qc.ExecuteWithMultipleMeasurements(1);
+	from_vector(qc.getRegisterStorage(), out);
 	return 0;
 }
 

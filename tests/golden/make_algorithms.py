@@ -8,8 +8,9 @@ Run in a checkout that has the QCSim sources (oracle/Makefile target `ref` build
 Each case is the state after the class's ExecuteWithoutMeasurement (GroverAlgorithm.h:89-98, DraperAdder.h:38-57 and
 :88-112, PhaseEstimation.h:195-215): Grover from its equal superposition with the given marked state; the adders from
 a random normalised superposition of inputs; phase estimation of a random unitary on the function register; VQE's
-PauliStringVQE Ansatz followed by Execute (VQE.h:33-114) from |0> with random parameters and operators; and Shor's
-period finding, ShorPhaseEstimation of Shor::Fx (PhaseEstimation.h:100-149, ShorAlgorithm.h:54-104).
+PauliStringVQE Ansatz followed by Execute (VQE.h:33-114) from |0> with random parameters and operators; Shor's
+period finding, ShorPhaseEstimation of Shor::Fx (PhaseEstimation.h:100-149, ShorAlgorithm.h:54-104); and quantum
+counting's pre-measurement state (QuantumCountingAlgorithm.h:104-128), read after its non-collapsing sampling.
 """
 from __future__ import annotations
 
@@ -33,6 +34,7 @@ VQE = [(1, 2), (2, 4), (3, 9), (4, 14), (5, 30)]  # (qubits, parameters): the an
 # (C, a, register qubits N, x qubits L); a^(2^(L-1)) must fit in 64 bits, since Fx squares in 64-bit arithmetic and
 # asserts that each modular multiplier is unitary (ShorAlgorithm.h:62-101)
 SHOR = [(15, 7, 7, 3), (15, 2, 7, 3), (15, 11, 7, 3), (21, 2, 11, 6)]
+COUNTING = [(3, 1, [5]), (4, 2, [0, 3]), (5, 3, [1, 2, 6, 7]), (6, 4, [0, 4, 9, 13, 15])]  # (P, G, marked states)
 
 
 def pd(a: np.ndarray):
@@ -49,7 +51,7 @@ def main() -> None:
     rng = np.random.default_rng(20261207)
     out = {"grover": np.array(GROVER, dtype=np.int64), "draper": np.array(DRAPER, dtype=np.int64),
            "phase": np.array(PHASE, dtype=np.int64), "vqe": np.array(VQE, dtype=np.int64),
-           "shor": np.array(SHOR, dtype=np.int64)}
+           "shor": np.array(SHOR, dtype=np.int64), "counting": np.array([c[:2] for c in COUNTING], dtype=np.int64)}
     for i, (n, marked) in enumerate(GROVER):
         res = np.zeros(1 << n, dtype=np.complex128)
         assert lib.qr_grover(n, marked, pd(res)) == 0
@@ -78,6 +80,11 @@ def main() -> None:
         res = np.zeros(1 << n, dtype=np.complex128)
         assert lib.qr_shor_period_finding(c, a, n, L, pd(res)) == 0
         out[f"shor{i}"] = res
+    for i, (P, Gq, marked) in enumerate(COUNTING):
+        mk = np.ascontiguousarray(marked, dtype=np.uint64)
+        res = np.zeros(1 << (P + 2 * Gq), dtype=np.complex128)
+        assert lib.qr_counting(P, Gq, len(marked), mk.ctypes.data_as(C.c_void_p), pd(res)) == 0
+        out[f"counting_marked{i}"], out[f"counting{i}"] = mk, res
     np.savez_compressed(OUT, **out)
     print("wrote", OUT, OUT.stat().st_size, "bytes")
 

@@ -505,7 +505,7 @@ def test_gate_built_oracles_match_reference(Q):
 
 def _check_algorithms_golden(A, make_reg, tol):
     """the mirrors' pre-measurement states against QCSim's own Grover search, Draper adders, phase estimation,
-    VQE ansatz and Shor's period finding
+    VQE ansatz, Shor's period finding and quantum counting
     (tests/golden/algorithms.npz, made by tests/golden/make_algorithms.py from the compiled reference)"""
     from pathlib import Path
     g = np.load(Path(__file__).resolve().parent / "golden" / "algorithms.npz")
@@ -546,6 +546,13 @@ def _check_algorithms_golden(A, make_reg, tol):
         A.ShorPhaseEstimation(fx, n, L).ExecuteWithoutMeasurement(reg)
         assert np.abs(reg.getRegisterStorage() - g[f"shor{i}"]).max() <= tol, ("shor", i)
         reg.close()
+    from qcsim_gb300 import counting as CT
+    for i, (P, Gq) in enumerate(g["counting"].tolist()):
+        qc = CT.QuantumCountingAlgorithm(P, Gq, seed=1)
+        qc.SetMarkedStates(g[f"counting_marked{i}"].tolist())
+        qc.ExecuteWithoutMeasurement()
+        assert np.abs(qc.getRegisterStorage() - g[f"counting{i}"]).max() <= tol, ("counting", i)
+        qc.close()
 
 
 def test_algorithms_match_reference(Q):
