@@ -126,7 +126,10 @@ int qcs_schrodinger_evolve(qcs_handle h, const double* potential_op, const doubl
 /* QuantumFourierTransform::QFT / IQFT on qubits [start, end] (QuantumFourierTransform.h:35-87) with
  * the mirror swaps of QubitsSwapper::Swap (QubitsSwapper.h:23-34) when do_swap != 0 */
 int qcs_qft(qcs_handle h, uint32_t start, uint32_t end, int inverse, int do_swap);
-/* OneQubitGateTransform (HadamardTransform.h:9-41): the same 1-qubit gate on every qubit in [start, end] */
+/* OneQubitGateTransform (HadamardTransform.h:9-41): the same 1-qubit gate on every qubit in [start, end].
+ * m is the gate's 2x2 matrix (row-major, interleaved) and traits its QCS_TRAIT_* bits.  start > end,
+ * end >= n or a null m return QCS_INVALID_ARGUMENT and leave the register unchanged (the reference's
+ * loop over an empty range does nothing; its callers clamp end to n - 1 first, QuantumAlgorithm.h:228-231). */
 int qcs_one_qubit_transform(qcs_handle h, const double* m, uint32_t traits, uint32_t start, uint32_t end);
 
 /* ---- measurement (QubitRegister.h:169-429, QubitRegisterCalculator.h:948-1254) ---- */
@@ -265,6 +268,10 @@ int qcs_profile_read(qcs_handle h, qcs_profile_entry* out, int capacity, int* co
 /* ---- engine statistics ---- */
 /* number of CUDA kernels this library has launched since it was loaded (all registers) */
 uint64_t qcs_launch_count(void);
+/* bytes of scratch the register has allocated for reductions and sampling so far: device memory
+ * (reduction partials, chunk sums, shot buffers) and pinned host memory.  Scratch is allocated on
+ * the register's first observation that needs it and kept until qcs_destroy. */
+int qcs_scratch_bytes(qcs_handle h, uint64_t* device_bytes, uint64_t* pinned_bytes);
 
 /* ---- host random stream: std::mt19937_64 + std::uniform_real_distribution<double>(0,1), the
  * generator and distribution of QubitRegister.h:723-724, for callers without a C++ runtime ---- */
@@ -274,19 +281,20 @@ int qcs_rng_destroy(qcs_rng_handle g);
 /* n uniforms in [0, 1) */
 int qcs_rng_uniform(qcs_rng_handle g, double* out, size_t n);
 
-/* ---- GetQubitProbability without device allocation ----
- * No reference counterpart: the reference's GetQubitProbability (QubitRegister.h:592-598) sums on
- * the host, and qcs_qubit_probability above is its replacement.  This variant gives the same value
- * (to rounding) but reduces through one fixed file-scope device array (256 KiB per GPU, resident
- * while the library is loaded) instead of scratch the register allocates, for callers that cannot
- * let the library allocate: a register that fills the GPU, device memory owned by the application's
- * own pool, or a loop that cannot take the device-wide wait of cudaFree.
+/* ---- qubit probability without device allocation ----
+ * No counterpart in the reference.  This variant of qcs_qubit_probability gives the same value (to
+ * rounding) but reduces through one fixed file-scope device array (256 KiB per GPU, resident while
+ * the library is loaded) instead of scratch the register allocates, for callers that cannot let the
+ * library allocate: a register that fills the GPU, device memory owned by the application's own
+ * pool, or a loop that cannot take the device-wide wait of cudaFree.
  *  - registers of at most 32 qubits; larger ones return QCS_UNSUPPORTED with a message;
  *  - call with the register's device current; the first call on a device sets the array up
  *    (address lookup, kernel loading), so make it before any stream capture on that device;
  *  - every call uses the same array: calls that can overlap on the GPU (registers on different
  *    streams, several host threads) race and must be serialised by the caller;
- *  - nothing needs zeroing first; blocks until the value is on the host. */
+ *  - nothing needs zeroing first;
+ *  - synchronous: it returns once the value has reached the host (a one-double device-to-host copy
+ *    and a synchronisation of the register's stream). */
 int qcs_qubit_probability_noalloc(qcs_handle h, uint32_t qubit, double* p_out);
 
 #ifdef __cplusplus

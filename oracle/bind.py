@@ -7,6 +7,7 @@ or the timed CPU baseline.
 from __future__ import annotations
 
 import ctypes as C
+import os
 import subprocess
 from pathlib import Path
 
@@ -15,7 +16,12 @@ import numpy as np
 HERE = Path(__file__).resolve().parent
 ORACLE_LIB = HERE / "libqcs_oracle.so"
 REF_LIB = HERE / "_ref" / "libqcsref.so"
-REF_DIR = Path("/root/reference/QCSim")
+# QCSim's sources as staged by `make -C oracle stage` (git-ignored, travels with the working tree)
+STAGED_SRC = HERE / "_ref" / "src"
+# ref_driver.cpp compiled against the GPU drop-in register, and QCSim's test suite on the drop-in
+DROPIN_LIB = HERE / "_ref" / "libqcsref_dropin.so"
+SUITE_BIN = HERE / "_ref" / "qcsim_tests_dropin"
+GPU_LIB = HERE.parent / "qcsim_gb300" / "libqcs_gpu.so"
 
 # qo_gate (oracle/qcs_oracle.h)
 QO_GATE = np.dtype([("code", "<i4"), ("q0", "<i4"), ("q1", "<i4"), ("q2", "<i4"), ("p", "<f8", (4,)),
@@ -45,6 +51,7 @@ _ORACLE_SIG = {
     "qo_expected_energy": (_d, [_h, _u32, _pu32, _pd, _pd]),
     "qo_rng_create": (_h, [_u64]), "qo_rng_destroy": (None, [_h]), "qo_rng_next": (_u64, [_h]),
     "qo_rng_uniform": (_d, [_h]),
+    "qo_random_normal_state": (None, [_u64, _u32, _pd]), "qo_max_abs_diff": (_d, [_pd, _pd, _u64]),
 }
 
 _REF_SIG = {
@@ -81,10 +88,26 @@ _oracle = None
 _ref = None
 
 
-def build_oracle(ref: bool = False) -> None:
-    """compile oracle/libqcs_oracle.so (and, if asked and the QCSim checkout is present, _ref)"""
-    targets = ["all"] + (["ref"] if ref and REF_DIR.exists() else [])
-    subprocess.run(["make", "-s", "-C", str(HERE), *targets], check=True)
+def qcsim_source() -> Path | None:
+    """the QCSim source directory named by the QCSIM_SRC environment variable, if it exists"""
+    s = os.environ.get("QCSIM_SRC")
+    return Path(s) if s and Path(s).is_dir() else None
+
+
+def build_oracle(ref: bool = False, dropin: bool = False) -> None:
+    """compile oracle/libqcs_oracle.so; with ref, also QCSim's own register (_ref/libqcsref.so); with
+    dropin, also ref_driver.cpp and QCSim's test suite over the GPU drop-in (needs libqcs_gpu.so).  The
+    QCSim sources are staged into _ref/src first when QCSIM_SRC names a checkout; the _ref targets are
+    built only where a staged copy exists."""
+    src = qcsim_source()
+    if (ref or dropin) and src is not None:
+        subprocess.run(["make", "-s", "-C", str(HERE), "stage", f"QCSIM_SRC={src}"], check=True)
+    targets = ["all"]
+    if STAGED_SRC.is_dir():
+        targets += ["ref"] if ref else []
+        targets += ["dropin"] if dropin and GPU_LIB.exists() else []
+    jobs = str(min(16, os.cpu_count() or 1))
+    subprocess.run(["make", "-s", f"-j{jobs}", "-C", str(HERE), *targets], check=True)
 
 
 def _bind(path: Path, sig: dict):
@@ -114,6 +137,22 @@ def ref():
     if _ref is None:
         _ref = _bind(REF_LIB, _REF_SIG)
     return _ref
+
+
+_ref_dropin = None
+
+
+def dropin_available() -> bool:
+    return DROPIN_LIB.exists()
+
+
+def ref_dropin():
+    """ref_driver.cpp's entry points over the GPU drop-in register: QCSim's own gate classes, algorithms
+    and sub-algorithms, unmodified, with every QC::QubitRegister backed by libqcs_gpu.so"""
+    global _ref_dropin
+    if _ref_dropin is None:
+        _ref_dropin = _bind(DROPIN_LIB, _REF_SIG)
+    return _ref_dropin
 
 
 def dp(a: np.ndarray):
@@ -172,10 +211,11 @@ class OracleRegister:
 
 
 class RefRegister:
-    """QCSim's own QubitRegister (compiled reference), seeded"""
+    """QCSim's own QubitRegister through ref_driver.cpp, seeded: the compiled reference (ref()), or the
+    same driver over the GPU drop-in register (ref_dropin())"""
 
-    def __init__(self, n: int, seed: int = 1):
-        self.lib = ref()
+    def __init__(self, n: int, seed: int = 1, lib=None):
+        self.lib = lib if lib is not None else ref()
         self.n = n
         self.N = 1 << n
         self.h = self.lib.qr_create(n, seed)

@@ -11,6 +11,7 @@
 #include <complex>
 #include <cstring>
 #include <limits>
+#include <random>
 #include <string>
 #include <vector>
 
@@ -709,5 +710,37 @@ void* qo_rng_create(uint64_t seed) { return new Mt64(seed); }
 void qo_rng_destroy(void* g) { delete static_cast<Mt64*>(g); }
 uint64_t qo_rng_next(void* g) { return static_cast<Mt64*>(g)->next(); }
 double qo_rng_uniform(void* g) { return static_cast<Mt64*>(g)->uniform(); }
+
+void qo_random_normal_state(uint64_t seed, uint32_t n, double* out) {
+	const uint64_t N = 1ULL << n;
+	const uint64_t block = std::min<uint64_t>(N, 1ULL << 20);
+	const long long nblocks = static_cast<long long>(N / block);
+	double norm2 = 0;
+#pragma omp parallel for reduction(+ : norm2) schedule(static)
+	for (long long b = 0; b < nblocks; ++b) {
+		std::mt19937_64 gen(seed * 1000003ULL + static_cast<uint64_t>(b));
+		std::normal_distribution<double> g(0.0, 1.0);
+		double acc = 0;
+		double* o = out + 2 * static_cast<uint64_t>(b) * block;
+		for (uint64_t i = 0; i < 2 * block; ++i) {
+			o[i] = g(gen);
+			acc += o[i] * o[i];
+		}
+		norm2 += acc;
+	}
+	const double inv = 1.0 / std::sqrt(norm2);
+#pragma omp parallel for schedule(static)
+	for (long long i = 0; i < static_cast<long long>(2 * N); ++i) out[i] *= inv;
+}
+
+double qo_max_abs_diff(const double* a, const double* b, uint64_t count) {
+	double worst = 0;
+#pragma omp parallel for reduction(max : worst) schedule(static)
+	for (long long i = 0; i < static_cast<long long>(count); ++i) {
+		const double dx = a[2 * i] - b[2 * i], dy = a[2 * i + 1] - b[2 * i + 1];
+		worst = std::max(worst, std::sqrt(dx * dx + dy * dy));
+	}
+	return worst;
+}
 
 }  // extern "C"

@@ -106,6 +106,14 @@ void qo_rng_destroy(void* g);
 uint64_t qo_rng_next(void* g);
 double qo_rng_uniform(void* g);
 
+/* bench inputs and checks at full size (OpenMP over all host threads):
+ * a random state a_x = (g1 + i g2) / norm, g iid N(0, 1) from std::normal_distribution<double> on
+ * std::mt19937_64; the 2^n amplitudes are drawn in blocks of 2^20, block b from the generator seeded
+ * with seed * 1000003 + b, so that the blocks can be drawn in parallel.  out: 2^n complex<double>. */
+void qo_random_normal_state(uint64_t seed, uint32_t n, double* out);
+/* max over i of |a_i - b_i| for `count` complex<double> entries */
+double qo_max_abs_diff(const double* a, const double* b, uint64_t count);
+
 #ifdef __cplusplus
 }
 #endif

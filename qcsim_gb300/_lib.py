@@ -127,6 +127,7 @@ SIGNATURES = {
     "qcs_profile_enable": (_i, [_h, _i]),
     "qcs_profile_read": (_i, [_h, C.c_void_p, _i, C.POINTER(_i)]),
     "qcs_launch_count": (_u64, []),
+    "qcs_scratch_bytes": (_i, [_h, C.POINTER(_u64), C.POINTER(_u64)]),
     "qcs_rng_create": (_i, [_u64, C.POINTER(_h)]),
     "qcs_rng_destroy": (_i, [_h]),
     "qcs_rng_uniform": (_i, [_h, _pd, _sz]),

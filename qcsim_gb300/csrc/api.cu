@@ -513,8 +513,12 @@ int qcs_qft(qcs_handle h, uint32_t start, uint32_t end, int inverse, int do_swap
 }
 
 int qcs_one_qubit_transform(qcs_handle h, const double* m, uint32_t traits, uint32_t start, uint32_t end) {
-	if (!h || !m) return QCS_INVALID_ARGUMENT;
+	if (!h) return QCS_INVALID_ARGUMENT;
+	if (!m) return fail(h, QCS_INVALID_ARGUMENT, "one-qubit transform: no gate matrix");
+	// the range is checked before the list is built: end < n also keeps q <= end from wrapping
+	if (end >= h->n || start > end) return fail(h, QCS_INVALID_ARGUMENT, "one-qubit transform: qubit range out of the register");
 	std::vector<qcs_gate> gs;
+	gs.reserve(end - start + 1);
 	for (uint32_t q = start; q <= end; ++q) {
 		qcs_gate g;
 		std::memset(&g, 0, sizeof(g));
@@ -737,6 +741,14 @@ void note_launches(uint64_t n) { g_launches.fetch_add(n, std::memory_order_relax
 }  // namespace qcs
 
 extern "C" uint64_t qcs_launch_count(void) { return qcs::g_launches.load(); }
+
+extern "C" int qcs_scratch_bytes(qcs_handle h, uint64_t* device_bytes, uint64_t* pinned_bytes) {
+	if (!h || !device_bytes || !pinned_bytes) return QCS_INVALID_ARGUMENT;
+	const qcs::Scratch& sc = h->sc;
+	*device_bytes = sizeof(double) * (sc.red_cap + sc.chunk_cap) + (sizeof(double) + sizeof(unsigned long long)) * sc.shot_cap;
+	*pinned_bytes = sizeof(double) * sc.pinned_cap;
+	return QCS_OK;
+}
 
 // exported for the batch planner: one gate through the per-gate kernels, and the scale fold
 namespace qcs {

@@ -15,6 +15,8 @@
 //  * The first call on a device does the set-up: it looks the array's address up with that device
 //    current and makes sure the kernels are loaded there.  Make that first call before any stream
 //    capture on the device.
+//  * Every call is synchronous: it copies the one-double result to the host and synchronises the
+//    register's stream before it returns.
 //  * All calls share the one array.  Calls whose kernels can overlap on the GPU (two registers on
 //    two streams, two host threads) race on it; serialise them.
 //  * Nothing has to start at zero: every slot a call reads was written earlier by the same call.

@@ -685,6 +685,12 @@ __global__ void __launch_bounds__(kTileThreads, 1) k_tile_tc(float2* __restrict_
 		}
 		__syncthreads();
 	}
+	if (stop) {
+		// an MMA completion wait ran out (the error flag is set; the register's state is then undefined
+		// and the host reports QCS_CUDA_ERROR): wait once more, again bounded, for the MMAs still in
+		// flight, so that their tensor memory is not released under them
+		tc::mbar_wait(&mbar_mma, mma_phase ^ 1u, kTcWaitTries);
+	}
 	tc::fence_before_sync();
 	__syncthreads();
 	if (warp == 0) tc::tmem_dealloc<kTcTmemCols>(tmem);

@@ -46,8 +46,13 @@ def unit(rng, n: int) -> np.ndarray:
     return np.ascontiguousarray(v / np.linalg.norm(v))
 
 
-def main() -> None:
-    lib = B.ref()
+def generate(lib=None, max_shor_qubits: int = 64) -> dict[str, np.ndarray]:
+    """every fixture array, produced through ref_driver.cpp's entry points in `lib` (default: the
+    compiled reference, B.ref(); B.ref_dropin() runs the same driver over the GPU drop-in register).
+    Shor cases on more than max_shor_qubits register qubits are left out: Fx builds its 2^N x 2^N
+    modular-multiplication operators as dense host matrices (the 11-qubit case spends about two minutes
+    in host matrix products, whichever register runs it)."""
+    lib = lib if lib is not None else B.ref()
     rng = np.random.default_rng(20261207)
     out = {"grover": np.array(GROVER, dtype=np.int64), "draper": np.array(DRAPER, dtype=np.int64),
            "phase": np.array(PHASE, dtype=np.int64), "vqe": np.array(VQE, dtype=np.int64),
@@ -77,6 +82,8 @@ def main() -> None:
                                pd(res)) == 0
         out[f"vqe_ops{i}"], out[f"vqe_params{i}"], out[f"vqe{i}"] = ops, params, res
     for i, (c, a, n, L) in enumerate(SHOR):
+        if n > max_shor_qubits:
+            continue
         res = np.zeros(1 << n, dtype=np.complex128)
         assert lib.qr_shor_period_finding(c, a, n, L, pd(res)) == 0
         out[f"shor{i}"] = res
@@ -85,7 +92,11 @@ def main() -> None:
         res = np.zeros(1 << (P + 2 * Gq), dtype=np.complex128)
         assert lib.qr_counting(P, Gq, len(marked), mk.ctypes.data_as(C.c_void_p), pd(res)) == 0
         out[f"counting_marked{i}"], out[f"counting{i}"] = mk, res
-    np.savez_compressed(OUT, **out)
+    return out
+
+
+def main() -> None:
+    np.savez_compressed(OUT, **generate())
     print("wrote", OUT, OUT.stat().st_size, "bytes")
 
 

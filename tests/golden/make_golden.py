@@ -29,9 +29,9 @@ PARAMS = (0.7, 0.3, -1.1, 0.25)
 C0_PROBE = 256  # amplitudes recorded from each 20-qubit state
 
 
-def uniforms(seed: int, n: int) -> np.ndarray:
+def uniforms(seed: int, n: int, lib=None) -> np.ndarray:
     u = np.zeros(n)
-    B.ref().qr_uniforms(seed, n, B.dp(u))
+    (lib if lib is not None else B.ref()).qr_uniforms(seed, n, B.dp(u))
     return u
 
 
@@ -45,10 +45,10 @@ def random_ops(rng: np.random.Generator, n: int, count: int, codes) -> list:
     return ops
 
 
-def main() -> None:
-    if not B.ref_available():
-        raise SystemExit("oracle/_ref/libqcsref.so missing: run `make -C oracle ref` in a QCSim checkout")
-    r = B.ref()
+def generate(lib=None) -> dict[str, np.ndarray]:
+    """every fixture array, produced through ref_driver.cpp's entry points in `lib` (default: the
+    compiled reference, B.ref(); B.ref_dropin() runs the same driver over the GPU drop-in register)"""
+    r = lib if lib is not None else B.ref()
     out: dict[str, np.ndarray] = {}
 
     # 1. gate matrices and traits of every reference gate class
@@ -78,7 +78,7 @@ def main() -> None:
                 qs = [int(x) for x in rng.choice(n, size=3, replace=False)]
                 ops.append((G.AppliedGate(q, *qs), *qs))
         recs = B.records(ops)
-        reg = B.RefRegister(n)
+        reg = B.RefRegister(n, lib=r)
         reg.apply(recs)
         circ_recs.append(recs)
         circ_n.append(n)
@@ -91,7 +91,7 @@ def main() -> None:
     # 3. layered circuit, 12 qubits, depth 10, Toffoli/CCZ at 5% of positions: full state, qubit
     #    probabilities, RepeatedMeasure(1024) with rng seed 7, then MeasureAll
     ops = circuits.layered_circuit(12, 10, seed=4, p3=0.05)
-    reg = B.RefRegister(12, seed=7)
+    reg = B.RefRegister(12, seed=7, lib=r)
     reg.apply(ops)
     out["l12_recs"] = B.records(ops)
     out["l12_state"] = reg.state()
@@ -107,7 +107,7 @@ def main() -> None:
     c0_amp, c0_qp, c0_hist, c0_norm = [], [], [], []
     for s in (1, 2, 3):
         ops = circuits.layered_circuit(20, 40, seed=s)
-        reg = B.RefRegister(20, seed=s)
+        reg = B.RefRegister(20, seed=s, lib=r)
         reg.apply(ops)
         st = reg.state()
         c0_amp.append(st[out["c0_probe_idx"]])
@@ -130,7 +130,7 @@ def main() -> None:
     states_after = []
     for s in range(16):
         for op in range(5):
-            reg = B.RefRegister(2, seed=1000 + s)
+            reg = B.RefRegister(2, seed=1000 + s, lib=r)
             reg.set_state(kat)
             r.qr_normalize(reg.h)
             if op == 0:
@@ -155,12 +155,12 @@ def main() -> None:
     out["sub_state"] = v
     sub_rows, sub_after, sub_hist = [], [], []
     for (a, b) in ((0, 0), (3, 5), (2, 9), (9, 9), (0, 9)):
-        reg = B.RefRegister(10, seed=31 + a * 10 + b)
+        reg = B.RefRegister(10, seed=31 + a * 10 + b, lib=r)
         reg.set_state(v)
         val = r.qr_measure(reg.h, a, b)
         sub_rows.append((a, b, val))
         sub_after.append(reg.state())
-        reg2 = B.RefRegister(10, seed=77 + a * 10 + b)
+        reg2 = B.RefRegister(10, seed=77 + a * 10 + b, lib=r)
         reg2.set_state(v)
         hh = reg2.repeated_measure(500, a, b)
         sub_hist.append(np.array([(a, b, k, c) for k, c in sorted(hh.items())], dtype=np.uint64))
@@ -174,7 +174,7 @@ def main() -> None:
     out["edge_state"] = w
     edge = []
     for s in range(12):
-        reg = B.RefRegister(10, seed=500 + s)
+        reg = B.RefRegister(10, seed=500 + s, lib=r)
         reg.set_state(w)
         a1 = r.qr_measure_no_collapse(reg.h)
         hh = reg.repeated_measure(64)
@@ -193,7 +193,7 @@ def main() -> None:
         else:
             st = rng.standard_normal(1 << n) + 1j * rng.standard_normal(1 << n)
             st /= np.linalg.norm(st)
-        reg = B.RefRegister(n)
+        reg = B.RefRegister(n, lib=r)
         reg.set_state(st)
         r.qr_qft(reg.h, n, s0, e0, inv, sw)
         qft_in.append(np.pad(st, (0, 512 - st.size)))
@@ -209,7 +209,7 @@ def main() -> None:
         e = np.array(inst["edges"], dtype=np.uint32).reshape(-1)
         J, hv = np.array(inst["J"]), np.array(inst["h"])
         gm, bt = np.array(inst["gammas"]), np.array(inst["betas"])
-        reg = B.RefRegister(n)
+        reg = B.RefRegister(n, lib=r)
         r.qr_qaoa_exec(reg.h, n, len(inst["edges"]), e.ctypes.data_as(C.POINTER(C.c_uint32)), B.dp(J), B.dp(hv),
                        len(gm), B.dp(gm), B.dp(bt))
         qa_states.append(np.pad(reg.state(), (0, 1024 - (1 << n))))
@@ -225,7 +225,7 @@ def main() -> None:
     ops = random_ops(rng, 6, 30, codes)
     exp_ops = random_ops(rng, 6, 5, [c for c in codes if c < 40])
     exp_gates = [(G.AppliedGate(g.getRawOperatorMatrix(), a, b, c), a, b, c) for (g, a, b, c) in exp_ops]
-    reg = B.RefRegister(6)
+    reg = B.RefRegister(6, lib=r)
     reg.apply(ops)
     re, im = C.c_double(), C.c_double()
     recs = B.records(exp_gates)
@@ -235,16 +235,22 @@ def main() -> None:
     out["exp_state_after"] = reg.state()
     replay = []
     for mode in (1, 2):
-        reg = B.RefRegister(6)
+        reg = B.RefRegister(6, lib=r)
         rr = B.records(ops)
         r.qr_record_and_replay(reg.h, rr.ctypes.data_as(C.c_void_p), len(rr), mode)
         replay.append(reg.state())
     out["replay_states"] = np.array(replay)
 
     # 11. the reference's random stream: uniforms of std::mt19937_64(seed) for three seeds
-    out["rng_uniforms"] = np.array([uniforms(s, 64) for s in (1, 7, 123456789)])
+    out["rng_uniforms"] = np.array([uniforms(s, 64, r) for s in (1, 7, 123456789)])
 
-    np.savez_compressed(OUT, **out)
+    return out
+
+
+def main() -> None:
+    if not B.ref_available():
+        raise SystemExit("oracle/_ref/libqcsref.so missing: run `make -C oracle ref` in a QCSim checkout")
+    np.savez_compressed(OUT, **generate())
     print(f"wrote {OUT} ({OUT.stat().st_size / 1024:.0f} KiB)")
 
 

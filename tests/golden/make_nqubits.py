@@ -33,8 +33,10 @@ def pd(a: np.ndarray):
     return a.view(np.float64).ctypes.data_as(C.POINTER(C.c_double))
 
 
-def main() -> None:
-    lib = B.ref()
+def generate(lib=None) -> dict[str, np.ndarray]:
+    """every fixture array, produced through ref_driver.cpp's entry points in `lib` (default: the
+    compiled reference, B.ref(); B.ref_dropin() runs the same driver over the GPU drop-in register)"""
+    lib = lib if lib is not None else B.ref()
     rng = np.random.default_rng(20261204)
     out = {"cases": np.array(CASES, dtype=np.int64)}
     for i, (n, k, ctrl) in enumerate(CASES):
@@ -43,7 +45,7 @@ def main() -> None:
         psi = np.ascontiguousarray(rng.standard_normal(nb) + 1j * rng.standard_normal(nb))
         psi /= np.linalg.norm(psi)
         ext = np.zeros((nb, nb), dtype=np.complex128)
-        reg = B.RefRegister(n)
+        reg = B.RefRegister(n, lib=lib)
         reg.set_state(psi)
         st = lib.qr_nqubits_gate(reg.h, n, pd(op), k, n - k, ctrl, pd(ext))
         assert st == 0
@@ -52,7 +54,11 @@ def main() -> None:
         if n <= 6:  # the extended matrices of the larger cases stay out of the fixture (size)
             out[f"ext{i}"] = ext
         out[f"out{i}"] = reg.state()
-    np.savez_compressed(OUT, **out)
+    return out
+
+
+def main() -> None:
+    np.savez_compressed(OUT, **generate())
     print("wrote", OUT, OUT.stat().st_size, "bytes")
 
 

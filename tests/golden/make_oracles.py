@@ -50,8 +50,10 @@ def table(kind: str, nin: int, nout: int, rng) -> np.ndarray:
     return rng.integers(0, 1 << nout, size).astype(np.uint64)
 
 
-def main() -> None:
-    lib = B.ref()
+def generate(lib=None) -> dict[str, np.ndarray]:
+    """every fixture array, produced through ref_driver.cpp's entry points in `lib` (default: the
+    compiled reference, B.ref(); B.ref_dropin() runs the same driver over the GPU drop-in register)"""
+    lib = lib if lib is not None else B.ref()
     rng = np.random.default_rng(20261206)
     out = {"cases": np.array([c[:6] for c in CASES], dtype=np.int64)}
     for i, (n, start, end, target, anc, simple, kind) in enumerate(CASES):
@@ -63,7 +65,11 @@ def main() -> None:
         assert lib.qr_oracle_with_gates(n, start, end, target, anc, simple, t.ctypes.data_as(C.c_void_p),
                                         res.view(np.float64).ctypes.data_as(C.POINTER(C.c_double))) == 0
         out[f"table{i}"], out[f"psi{i}"], out[f"out{i}"] = t, psi, res
-    np.savez_compressed(OUT, **out)
+    return out
+
+
+def main() -> None:
+    np.savez_compressed(OUT, **generate())
     print("wrote", OUT, OUT.stat().st_size, "bytes")
 
 

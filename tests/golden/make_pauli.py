@@ -31,8 +31,10 @@ def pd(a: np.ndarray):
     return a.view(np.float64).ctypes.data_as(C.POINTER(C.c_double))
 
 
-def main() -> None:
-    lib = B.ref()
+def generate(lib=None) -> dict[str, np.ndarray]:
+    """every fixture array, produced through ref_driver.cpp's entry points in `lib` (default: the
+    compiled reference, B.ref(); B.ref_dropin() runs the same driver over the GPU drop-in register)"""
+    lib = lib if lib is not None else B.ref()
     rng = np.random.default_rng(20261205)
     out = {"cases": np.array([c[:2] for c in CASES], dtype=np.int64), "times": np.array([c[2] for c in CASES]),
            "steps": np.array([c[3] for c in CASES], dtype=np.int64)}
@@ -46,7 +48,11 @@ def main() -> None:
                                      t, steps, pd(res))
         assert st == 0
         out[f"psi{i}"], out[f"ops{i}"], out[f"coeffs{i}"], out[f"out{i}"] = psi, ops, coeffs, res
-    np.savez_compressed(OUT, **out)
+    return out
+
+
+def main() -> None:
+    np.savez_compressed(OUT, **generate())
     print("wrote", OUT, OUT.stat().st_size, "bytes")
 
 

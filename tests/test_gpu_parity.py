@@ -574,3 +574,48 @@ def test_largest_registers(Q, n, precision):
     assert reg.GetQubitProbability(5) < tol
     assert abs(reg.getBasisStateAmplitude((1 << top) | (1 << 17) | (1 << 9)) - 0.5) < tol
     reg.close()
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_one_qubit_transforms(Q, precision):
+    """OneQubitGateTransform, HadamardTransform and XTransform (HadamardTransform.h:9-41) on sub-ranges
+    [start, end] of a random state, against the oracle applying the reference's loop gate by gate;
+    end beyond the register is clamped to n - 1 as QuantumSubAlgorithmOnSubregister does
+    (QuantumAlgorithm.h:228-231).  FP64 1e-12, FP32 2e-6."""
+    from qcsim_gb300 import gates as G, subalgo as S
+    tol = TOL if precision == "fp64" else 2e-6
+    for n in (7, 16):  # 16 qubits: the gate lists go through the shared-memory passes
+        init = rand_state(n, n)
+        reg = Q.QubitRegister(n, seed=1, precision=precision)
+        ry = G.RyGate(0.83)
+        for cls, gate, start, end in ((S.HadamardTransform, None, 0, S.INT_MAX), (S.XTransform, None, 2, n - 3),
+                                      (S.OneQubitGateTransform, ry, 1, n + 5), (S.HadamardTransform, None, n - 1, n - 1),
+                                      (S.OneQubitGateTransform, G.TGate(), 3, 3)):
+            t = cls(n, start, end) if gate is None else cls(n, start, end, gate=gate)
+            g = t.gate
+            reg.setRegisterStorageFastNoNormalize(init)
+            t.Execute(reg)
+            ops = [(g, q) for q in range(t.getStartQubit(), t.getEndQubit() + 1)]
+            err = float(np.abs(reg.getRegisterStorage() - oracle_state(n, ops, init)).max())
+            assert err <= tol, (cls.__name__, start, end, err)
+        reg.close()
+
+
+def test_one_qubit_transform_rejects_bad_ranges(Q):
+    """the C ABI rejects start > end, end >= n and a missing matrix before building the gate list, and
+    leaves the state unchanged"""
+    import ctypes as C
+    from qcsim_gb300 import _lib as L, gates as G
+    lib = L.load()
+    n = 6
+    reg = Q.QubitRegister(n, seed=1)
+    init = rand_state(n, 3)
+    reg.setRegisterStorageFastNoNormalize(init)
+    m = np.ascontiguousarray(G.HadamardGate().getRawOperatorMatrix(), dtype=np.complex128)
+    pm = m.view(np.float64).ctypes.data_as(C.POINTER(C.c_double))
+    tr = G.HadamardGate().traits()
+    for start, end in ((3, 2), (0, n), (0, 0xFFFFFFFF), (n, n)):
+        assert lib.qcs_one_qubit_transform(reg.handle, pm, tr, start, end) == L.QCS_INVALID_ARGUMENT
+    assert lib.qcs_one_qubit_transform(reg.handle, None, tr, 0, 1) == L.QCS_INVALID_ARGUMENT
+    assert np.abs(reg.getRegisterStorage() - init).max() == 0.0
+    reg.close()

@@ -11,6 +11,7 @@ import pytest
 from qcsim_gb300 import _lib as L
 from qcsim_gb300 import circuits, gates as G
 from qcsim_gb300.rng import Mt19937_64
+from oracle import bind
 
 ROOT = Path(__file__).resolve().parents[1]
 
@@ -107,10 +108,10 @@ def test_engine_rng_matches_reference(golden):
         assert np.array_equal(Rng(seed).uniform(row.size), row)
 
 
-REF_QCSIM = Path("/root/reference/QCSim")
+REF_QCSIM = bind.STAGED_SRC
 
 
-@pytest.mark.skipif(not REF_QCSIM.exists(), reason="needs the QCSim sources")
+@pytest.mark.skipif(not REF_QCSIM.is_dir(), reason="needs QCSim's sources staged by make -C oracle stage")
 @pytest.mark.parametrize("program", ["dropin_check", "dropin_algorithms"])
 def test_cpp_dropin_compiles_against_reference_headers(program):
     """QCSim's own algorithm headers, unmodified, compile and link against the GPU-backed QubitRegister.h
@@ -234,3 +235,13 @@ def test_records_match_to_record():
         G.to_record(op[0], qs[0], qs[1], qs[2], out=want[i])
     assert G.records(ops).tobytes() == want.tobytes()
     assert G.records([]).size == 0
+
+
+@pytest.mark.skipif(not bind.DROPIN_LIB.exists(), reason="needs QCSim's sources staged and make -C oracle dropin")
+def test_reference_driver_builds_on_the_dropin():
+    """ref_driver.cpp compiled against the drop-in register loads (no GPU call) and exports the same entry
+    points as the compiled reference, and QCSim's test-suite program over the drop-in is built"""
+    lib = C.CDLL(str(bind.DROPIN_LIB))
+    missing = [name for name in bind._REF_SIG if not hasattr(lib, name)]
+    assert not missing, missing
+    assert bind.SUITE_BIN.exists()

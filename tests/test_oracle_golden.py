@@ -223,3 +223,27 @@ def test_invalid_arguments(oracle_lib):
                      ([(G.ToffoliGate(), 0, 1, 1)], "Qubits must be different")):
         with pytest.raises(ValueError, match=msg):
             reg.apply(ops)
+
+
+@pytest.mark.skipif(not B.REF_LIB.exists(), reason="the compiled reference (make -C oracle ref) is not built")
+@pytest.mark.parametrize("generator,fixture", [("make_golden", "golden"), ("make_oracles", "oracles"),
+                                               ("make_pauli", "pauli"), ("make_nqubits", "nqubits")])
+def test_compiled_reference_reproduces_fixtures(generator, fixture):
+    """the committed fixtures are what the generators make from QCSim's own register, compiled here:
+    integer outputs (shots, histograms, records) exactly, floating-point ones to 1e-15 (OpenMP reduction
+    order of the probability sums)"""
+    import importlib
+    import sys
+    from pathlib import Path
+    golden_dir = Path(__file__).resolve().parent / "golden"
+    if str(golden_dir) not in sys.path:
+        sys.path.insert(0, str(golden_dir))
+    out = importlib.import_module(generator).generate(B.ref())
+    want = np.load(golden_dir / f"{fixture}.npz")
+    assert set(out) == set(want.files)
+    for k, a in out.items():
+        a, b = np.asarray(a), want[k]
+        if a.dtype.kind in "iuV":
+            assert np.array_equal(a, b), k
+        elif a.size:
+            assert float(np.abs(a - b).max()) <= 1e-15, k
