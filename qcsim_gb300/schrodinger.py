@@ -19,7 +19,7 @@ from concurrent.futures import ThreadPoolExecutor
 
 import numpy as np
 
-from .algorithms import QuantumAlgorithm
+from .subalgo import QuantumAlgorithm
 
 
 def _polar(t: np.ndarray) -> np.ndarray:

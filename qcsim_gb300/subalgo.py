@@ -1,5 +1,6 @@
-"""QCSim's sub-algorithms of the statevector hot path over the engine register: QubitsSwapper
-(QubitsSwapper.h:10-43), QuantumFourierTransform (QuantumFourierTransform.h:12-92),
+"""QCSim's algorithm base and the sub-algorithms of the statevector hot path over the engine register:
+QuantumAlgorithm (QuantumAlgorithm.h:9-205, the owner of a register that its algorithms derive from),
+QubitsSwapper (QubitsSwapper.h:10-43), QuantumFourierTransform (QuantumFourierTransform.h:12-92),
 OneQubitGateTransform / HadamardTransform / XTransform (HadamardTransform.h:9-41), and the dense operator
 gates NQubitsQuantumGate (NQubitsQuantumGate.h:9-78) / NQubitsControlledQuantumGate
 (NQubitsControlledQuantumGate.h:9-97), on the qubit range of QuantumSubAlgorithmOnSubregister
@@ -16,6 +17,7 @@ import ctypes as C
 import numpy as np
 
 from . import gates as G
+from .register import QubitRegister
 
 INT_MAX = 2**31 - 1
 
@@ -183,3 +185,97 @@ class NQubitsControlledQuantumGate(NQubitsQuantumGate):
 
     def getNrQubits(self) -> int:
         return self.nrQubits
+
+
+class QuantumAlgorithm:
+    """QC::QuantumAlgorithm (QuantumAlgorithm.h:9-205): owns the register and forwards the state setters,
+    gates, measurements and record / replay to it"""
+
+    def __init__(self, N: int = 3, addseed: int = 0, *, precision: str = "fp64", seed: int | None = None):
+        self.reg = QubitRegister(N, addseed, precision=precision, seed=seed)
+
+    def getNrQubits(self) -> int:
+        return self.reg.getNrQubits()
+
+    def getNrBasisStates(self) -> int:
+        return self.reg.getNrBasisStates()
+
+    def getBasisStateAmplitude(self, State: int) -> complex:
+        return self.reg.getBasisStateAmplitude(State)
+
+    def getBasisStateProbability(self, State: int) -> float:
+        return self.reg.getBasisStateProbability(State)
+
+    def setToBasisState(self, State: int) -> None:
+        self.reg.setToBasisState(State)
+
+    def setToQubitState(self, q: int) -> None:
+        self.reg.setToQubitState(q)
+
+    def setToCatState(self) -> None:
+        self.reg.setToCatState()
+
+    def setToEqualSuperposition(self) -> None:
+        self.reg.setToEqualSuperposition()
+
+    def setRawAmplitude(self, State: int, val: complex) -> None:
+        self.reg.setRawAmplitude(State, val)
+
+    def Clear(self) -> None:
+        self.reg.Clear()
+
+    def Normalize(self) -> None:
+        self.reg.Normalize()
+
+    def AdjustPhaseAndNormalize(self) -> None:
+        self.reg.AdjustPhaseAndNormalize()
+
+    def getRegister(self) -> QubitRegister:
+        return self.reg
+
+    def getRegisterStorage(self) -> np.ndarray:
+        return self.reg.getRegisterStorage()
+
+    def setRegisterStorage(self, vals) -> None:
+        self.reg.setRegisterStorage(vals)
+
+    def ApplyGate(self, gate, qubit=None, controllingQubit: int = 0, controllingQubit2: int = 0) -> None:
+        self.reg.ApplyGate(gate, qubit, controllingQubit, controllingQubit2)
+
+    def ApplyGates(self, gates) -> None:
+        self.reg.ApplyGates(gates)
+
+    def ApplyOperatorMatrix(self, m) -> None:
+        self.reg.ApplyOperatorMatrix(m)
+
+    def RepeatedMeasure(self, *args) -> dict:
+        return self.reg.RepeatedMeasure(*args)
+
+    def Measure(self, *args) -> int:
+        """Measure() = MeasureAll, Measure(q) = MeasureQubit, Measure(first, second) (QuantumAlgorithm.h:121-135)"""
+        if not args:
+            return self.reg.MeasureAll()
+        if len(args) == 1:
+            return self.reg.MeasureQubit(args[0])
+        return self.reg.Measure(args[0], args[1])
+
+    def stateFidelity(self, state) -> float:
+        return self.reg.stateFidelity(state)
+
+    def ComputeStart(self) -> None:
+        self.reg.ComputeStart()
+
+    def ComputeEnd(self) -> None:
+        self.reg.ComputeEnd()
+
+    def ComputeClear(self) -> None:
+        self.reg.ComputeClear()
+
+    def Compute(self) -> None:
+        self.reg.Compute()
+
+    def Uncompute(self) -> None:
+        self.reg.Uncompute()
+
+    def close(self) -> None:
+        self.reg.close()

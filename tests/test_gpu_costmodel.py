@@ -92,10 +92,14 @@ def test_apply_matrix_any_order(cm):
     _ = (G, oracle_state)
 
 
+LEARNED_MARGIN = 0.97  # the learned partition's time must be at most this fraction of the best greedy fuser's
+
+
 def test_trained_model_beats_the_fixed_fuser(cm):
-    """the committed, GPU-trained cost model against the method without it (the greedy fuser with its
-    default largest block of 5 qubits) on an unseen 26-qubit circuit with controlled rotations: the
-    learned partition must run faster, and both FP32 results stay within 1-F <= 1e-6 of the FP64 path"""
+    """the committed, GPU-trained cost model against the method without it: the greedy fuser at its best
+    largest block (3 or 5 qubits, whichever runs faster here), on an unseen 26-qubit circuit of depth 12
+    with 10% controlled rotations.  The learned partition must take at most LEARNED_MARGIN of the
+    faster greedy fuser's time, and every FP32 result stays within 1-F <= 1e-6 of the FP64 path."""
     import ctypes as C
     import torch
     from qcsim_gb300 import QubitRegister, _lib as L, circuits, gates as G
@@ -126,7 +130,10 @@ def test_trained_model_beats_the_fixed_fuser(cm):
         reg.close()
         return best, 1.0 - f.value
 
-    t_greedy, inf_greedy = run(lambda r: r.set_fusion(1, 5))
+    t_greedy5, inf_greedy5 = run(lambda r: r.set_fusion(1, 5))
+    t_greedy3, inf_greedy3 = run(lambda r: r.set_fusion(1, 3))
     t_learned, inf_learned = run(lambda r: cm.attach(r, mlp, pass_ms))
-    assert inf_greedy <= 1e-6 and inf_learned <= 1e-6
-    assert t_learned < 0.8 * t_greedy, (t_learned, t_greedy)
+    assert max(inf_greedy5, inf_greedy3, inf_learned) <= 1e-6
+    t_best = min(t_greedy3, t_greedy5)
+    print(f"learned {t_learned:.2f} ms, greedy<=3 {t_greedy3:.2f} ms, greedy<=5 {t_greedy5:.2f} ms")
+    assert t_learned <= LEARNED_MARGIN * t_best, (t_learned, t_greedy3, t_greedy5)

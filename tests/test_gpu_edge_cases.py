@@ -45,7 +45,7 @@ def test_empty_inputs(Q, n, precision):
 
 def test_one_qubit_register(Q):
     from oracle import bind as B
-    from qcsim_gb300 import algorithms as A, gates as G
+    from qcsim_gb300 import subalgo as A, gates as G
     for precision, tol in (("fp64", 1e-15), ("fp32", 1e-7)):
         reg = Q.QubitRegister(1, seed=3, precision=precision)
         reg.ApplyGate(G.HadamardGate(), 0)

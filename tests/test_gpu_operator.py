@@ -36,7 +36,7 @@ def rand_state(rng, n):
 
 @pytest.mark.parametrize("precision", ["fp64", "fp32"])
 def test_nqubits_gates_match_reference(Q, precision):
-    from qcsim_gb300 import algorithms as A
+    from qcsim_gb300 import subalgo as A
     fx = np.load(FX)
     tol = 1e-13 if precision == "fp64" else 2e-6
     for i, (n, k, ctrl) in enumerate(fx["cases"]):
@@ -96,7 +96,7 @@ def test_operator_on_larger_register(Q):
 def test_recording_register_keeps_the_extended_matrix(Q):
     """with gate recording on, Execute logs and applies the extended matrix as the reference does; the
     result equals the device path's"""
-    from qcsim_gb300 import algorithms as A
+    from qcsim_gb300 import subalgo as A
     rng = np.random.default_rng(4)
     n, k = 7, 3
     op, psi = rand_op(rng, k), rand_state(rng, n)

@@ -183,27 +183,27 @@ def test_scan_edges(Q, golden):
 
 
 def test_qft(Q, golden):
-    from qcsim_gb300 import algorithms
+    from qcsim_gb300 import subalgo
     for cfg, inp, outp in zip(golden["qft_cfg"], golden["qft_in"], golden["qft_out"]):
         n, s0, e0, inv, sw = (int(x) for x in cfg)
         reg = Q.QubitRegister(n, seed=1)
         reg.setRegisterStorageFastNoNormalize(inp[: 1 << n])
-        qft = algorithms.QuantumFourierTransform(n, s0, e0)
+        qft = subalgo.QuantumFourierTransform(n, s0, e0)
         (qft.IQFT if inv else qft.QFT)(reg, bool(sw))
         assert np.abs(reg.getRegisterStorage() - outp[: 1 << n]).max() <= TOL
 
 
 @pytest.mark.parametrize("n", [12, 18])
 def test_qft_random_state(Q, n):
-    from qcsim_gb300 import algorithms, circuits
+    from qcsim_gb300 import circuits, subalgo
     v = circuits.random_normal_state(n, 5)
     reg = Q.QubitRegister(n, seed=1)
     reg.setRegisterStorageFastNoNormalize(v)
-    algorithms.QuantumFourierTransform(n).QFT(reg)
+    subalgo.QuantumFourierTransform(n).QFT(reg)
     want = oracle_state(n, circuits.qft_circuit(0, n - 1), v)
     assert np.abs(reg.getRegisterStorage() - want).max() <= TOL
     # QFT then IQFT returns the input
-    algorithms.QuantumFourierTransform(n).IQFT(reg)
+    subalgo.QuantumFourierTransform(n).IQFT(reg)
     assert np.abs(reg.getRegisterStorage() - v).max() <= 1e-11
 
 
@@ -354,12 +354,12 @@ def test_passes_match_per_gate(Q, n, precision):
 
 
 def test_qft_passes(Q):
-    from qcsim_gb300 import algorithms, circuits
+    from qcsim_gb300 import circuits, subalgo
     n = 20
     v = circuits.random_normal_state(n, 11)
     reg = Q.QubitRegister(n, seed=1)
     reg.setRegisterStorageFastNoNormalize(v)
-    algorithms.QuantumFourierTransform(n).QFT(reg)
+    subalgo.QuantumFourierTransform(n).QFT(reg)
     got = reg.getRegisterStorage()
     # QFT|v> is the unitary DFT with e^{+2 pi i jk / N}: N * ifft(v) / sqrt(N) (the bit-reversing swaps included)
     want = np.fft.ifft(v) * np.sqrt(v.size)
@@ -373,7 +373,7 @@ def test_qft_phase_rows(Q, start, end, precision):
     """QFT / IQFT on a sub-register of an 18-qubit register (shared-memory passes, each target's run of
     controlled phases applied as one row; FP32 registers too, whose gate lists are otherwise fused)
     against the oracle's gate-by-gate sequence"""
-    from qcsim_gb300 import algorithms, circuits
+    from qcsim_gb300 import circuits, subalgo
     n = 18
     tol = TOL if precision == "fp64" else 2e-6
     v = circuits.random_normal_state(n, 21 + start + end)
@@ -381,7 +381,7 @@ def test_qft_phase_rows(Q, start, end, precision):
         for do_swap in (False, True):
             reg = Q.QubitRegister(n, seed=1, precision=precision)
             reg.setRegisterStorageFastNoNormalize(v)
-            qft = algorithms.QuantumFourierTransform(n, start, end)
+            qft = subalgo.QuantumFourierTransform(n, start, end)
             (qft.IQFT if inverse else qft.QFT)(reg, do_swap)
             want = oracle_state(n, circuits.qft_circuit(start, end, inverse=inverse, do_swap=do_swap), v)
             assert np.abs(reg.getRegisterStorage() - want).max() <= tol, (inverse, do_swap)
@@ -450,10 +450,10 @@ def test_full_size_round_trips(Q, n, precision, depth):
     """the configurations' full sizes (30 qubits FP64 = 16 GiB; 33 qubits FP32 = 64 GiB, fused path with
     tensor-core blocks) through size-independent properties: QFT|0> is the uniform state, a layered
     circuit followed by its inverse and the inverse QFT return |0>"""
-    from qcsim_gb300 import algorithms, circuits
+    from qcsim_gb300 import circuits, subalgo
     tol = 1e-10 if precision == "fp64" else 2e-4
     reg = Q.QubitRegister(n, seed=1, precision=precision)
-    qft = algorithms.QuantumFourierTransform(n)
+    qft = subalgo.QuantumFourierTransform(n)
     qft.QFT(reg)
     u = 2.0 ** (-n / 2)
     for idx in (0, 1, (1 << n) - 1, 0x2AAAAAAA & ((1 << n) - 1)):

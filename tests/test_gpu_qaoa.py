@@ -105,46 +105,3 @@ def test_autotune_schedule_invariant(qaoa, precision, tmp_path):
     assert f"{batch.cluster},{batch.tile[0]},{batch.tile[1]}" == best
     other = qaoa.QaoaBatch(insts, 2, precision)
     assert other.autotune(cache=cache) == times and other.cluster == batch.cluster and other.tile == batch.tile
-
-
-def test_ising_subalgorithm_exec_matches_oracle(qaoa):
-    """Models::QAOAIsingSubalgorithm::Exec (IsingModel.h:557-567) on one engine register, as one gate list,
-    against the oracle's QAOA circuit"""
-    from qcsim_gb300 import QubitRegister, circuits
-    from qcsim_gb300 import ising as I
-    for inst in circuits.qaoa_instances(3, seed=5, nmin=8, nmax=14, p=3):
-        q = I.QAOAIsingSubalgorithm()
-        q.Set([(i, j, J) for (i, j), J in zip(inst["edges"], inst["J"])], inst["h"])
-        reg = QubitRegister(inst["n"], seed=1)
-        q.Exec(reg, inst["gammas"], inst["betas"])
-        st, _ = oracle_run(inst)
-        assert np.abs(reg.getRegisterStorage() - st).max() <= 1e-12
-        reg.close()
-
-
-def test_ising_subalgorithm_optimiser(qaoa):
-    """IsingTests.cpp: IsingModelTest (3 spins, p = 3, better mixing) returns the ground state and MaxCutTest
-    (6 vertices, p = 2) a maximum cut, with every sampled energy drawn from the engine register"""
-    from qcsim_gb300 import QubitRegister
-    from qcsim_gb300 import ising as I
-    q = I.QAOAIsingSubalgorithm()
-    q.Set([(0, 1, 1.5), (1, 2, 2), (0, 2, -3)], [1.25, 3.25, -2.5])
-    q.SetP(3)
-    q.SetGammaStart(1)
-    q.SetBetaStart(3)
-    q.SetGammaStart(0.3, 1)
-    q.SetBetaStart(1, 1)
-    q.SetMixing(True)
-    reg = QubitRegister(3, seed=4)
-    assert q.Execute(reg) == q.GetMinEnergyState()
-    reg.close()
-    m = I.QAOAIsingSubalgorithm()
-    m.Set([(0, 1, -1), (0, 2, -1), (0, 5, -1), (1, 2, -1), (1, 3, -1), (2, 3, -1), (2, 4, -1), (3, 5, -1)], [0.0] * 6)
-    m.SetP(2)
-    m.SetGammaStart(6)
-    m.SetBetaStart(0.7)
-    m.SetGammaStart(4.2, 1)
-    m.SetBetaStart(0.5, 1)
-    reg = QubitRegister(6, seed=4)
-    assert m.Execute(reg) in m.GetMinEnergyStates()
-    reg.close()

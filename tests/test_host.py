@@ -108,37 +108,6 @@ def test_engine_rng_matches_reference(golden):
         assert np.array_equal(Rng(seed).uniform(row.size), row)
 
 
-REF_QCSIM = bind.STAGED_SRC
-
-
-@pytest.mark.skipif(not REF_QCSIM.is_dir(), reason="needs QCSim's sources staged by make -C oracle stage")
-@pytest.mark.parametrize("program", ["dropin_check", "dropin_algorithms"])
-def test_cpp_dropin_compiles_against_reference_headers(program):
-    """QCSim's own algorithm headers, unmodified, compile and link against the GPU-backed QubitRegister.h
-    of qcsim_gb300/cpp: QFT, Grover, Draper adder, QAOA and phase estimation (dropin_check.cpp); Shor,
-    VQE, error correction, Bernstein-Vazirani, Deutsch-Jozsa, Simon, superdense coding, teleportation,
-    quantum counting, the adders, q-means, CHSH and BB84 (dropin_algorithms.cpp).  The reference's quoted
-    includes are resolved through the include path (-I-), so the drop-in headers win."""
-    import glob
-    import shutil
-    import subprocess
-    if not L.LIB_PATH.exists():
-        pytest.skip("libqcs_gpu.so not built")
-    gxx = shutil.which("g++")
-    if not gxx:
-        pytest.skip("no g++")
-    pstl = sorted(glob.glob("/usr/include/c++/*/pstl"))
-    out = ROOT / "qcsim_gb300" / "_build"
-    out.mkdir(exist_ok=True)
-    cmd = [gxx, "-std=c++17", "-O1", f"-I{ROOT / 'qcsim_gb300' / 'cpp'}", f"-I{ROOT / 'include'}", f"-I{REF_QCSIM}", "-I-",
-           f"-I{ROOT / 'oracle' / 'eigen_shim'}"] + [f"-I{p}" for p in pstl[-1:]] + [
-           str(ROOT / "tests" / "cpp" / f"{program}.cpp"), "-o", str(out / program),
-           f"-L{L.LIB_PATH.parent}", "-lqcs_gpu", f"-Wl,-rpath,{L.LIB_PATH.parent}"]
-    r = subprocess.run(cmd, capture_output=True, text=True)
-    assert r.returncode == 0, r.stderr[-3000:]
-    assert (out / program).exists()
-
-
 def test_fusion_plan_covers_every_gate():
     """the greedy fuser (host code of the engine) keeps every gate, in blocks no wider than asked
     unless a single gate is wider"""

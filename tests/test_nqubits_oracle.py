@@ -6,7 +6,7 @@ import numpy as np
 import pytest
 
 from oracle import nqubits as O
-from qcsim_gb300 import algorithms as A
+from qcsim_gb300 import subalgo as A
 
 ROOT_GOLDEN = __import__("pathlib").Path(__file__).resolve().parent / "golden" / "nqubits.npz"
 
