@@ -138,6 +138,16 @@ int sample_any(qcs_handle h, const double* probs, size_t n, int mode, uint64_t f
 	return QCS_OK;
 }
 
+// a register of at most kSmallMeasure amplitudes: sampling and collapse in one launch (measure_small)
+int measure_small_any(qcs_handle h, double prob, uint64_t mask, int kind, uint64_t fallback, uint64_t* out) {
+	if (int st = materialize(h)) return st;
+	cudaError_t e = h->prec == QCS_FP64
+	                    ? qcs::measure_small<double>(static_cast<double2*>(h->d_state), h->N, prob, mask, kind, fallback, h->sc, h->stream, out)
+	                    : qcs::measure_small<float>(static_cast<float2*>(h->d_state), h->N, prob, mask, kind, fallback, h->sc, h->stream, out);
+	QCS_CK(h, e, "measurement");
+	return QCS_OK;
+}
+
 int set_basis_impl(qcs_handle h, uint64_t state) {
 	if (state < h->N) h->scale = cd(1, 0);
 	if (state >= h->N) return QCS_OK;
@@ -533,6 +543,7 @@ int qcs_one_qubit_transform(qcs_handle h, const double* m, uint32_t traits, uint
 
 int qcs_measure_all(qcs_handle h, double prob, uint64_t* state_out) {
 	if (!h || !state_out) return QCS_INVALID_ARGUMENT;
+	if (h->N <= qcs::kSmallMeasure) return measure_small_any(h, prob, 0, 1, h->N - 1, state_out);
 	uint64_t st = 0;
 	int r = sample_any(h, &prob, 1, 0, h->N - 1, &st);
 	if (r) return r;
@@ -547,6 +558,11 @@ int qcs_measure(qcs_handle h, uint32_t first, uint32_t second, double prob, uint
 	const uint64_t firstMask = (1ULL << first) - 1;
 	const uint64_t mask = (1ULL << (second + 1)) - 1 - firstMask;
 	uint64_t st = 0;
+	if (h->N <= qcs::kSmallMeasure) {
+		if (int r = measure_small_any(h, prob, mask, 0, 0, &st)) return r;
+		*value_out = (st & mask) >> first;
+		return QCS_OK;
+	}
 	int r = sample_any(h, &prob, 1, 0, 0, &st);
 	if (r) return r;
 	const uint64_t picked = st & mask;
@@ -559,6 +575,7 @@ int qcs_measure(qcs_handle h, uint32_t first, uint32_t second, double prob, uint
 
 int qcs_measure_no_collapse(qcs_handle h, double prob, uint64_t* state_out) {
 	if (!h || !state_out) return QCS_INVALID_ARGUMENT;
+	if (h->N <= qcs::kSmallMeasure) return measure_small_any(h, prob, 0, 2, 0, state_out);
 	return sample_any(h, &prob, 1, 0, 0, state_out);
 }
 

@@ -147,6 +147,63 @@ void push_block_tc(std::vector<float2>& mats, const std::vector<std::complex<dou
 	for (size_t k = 0; k < f.size(); k += 2) mats.push_back(make_float2(f[k], f[k + 1]));
 }
 
+// a fused block on fewer than 4 tile positions, widened to 4 by the lowest tile positions it does not
+// use (identity on them), for the tensor-core pass; pos becomes the ascending positions of the result,
+// and the returned matrix has bit t <-> pos[t]
+std::vector<std::complex<double>> pad_block(std::vector<int>& pos, const std::vector<std::complex<double>>& M, int k) {
+	std::vector<int> all = pos;
+	for (int b = 0; b < k && all.size() < 4; ++b)
+		if (std::find(all.begin(), all.end(), b) == all.end()) all.push_back(b);
+	std::sort(all.begin(), all.end());
+	const uint32_t d = 1u << pos.size();
+	std::vector<uint32_t> inner(all.size(), 0);  // bit t of the new index: bit of the old matrix, or 0 (extra)
+	uint32_t extra = 0;
+	for (size_t t = 0; t < all.size(); ++t) {
+		const auto it = std::find(pos.begin(), pos.end(), all[t]);
+		if (it != pos.end()) inner[t] = 1u << static_cast<uint32_t>(it - pos.begin());
+		else extra |= 1u << t;
+	}
+	auto old_index = [&](uint32_t i) {
+		uint32_t o = 0;
+		for (size_t t = 0; t < all.size(); ++t)
+			if ((i >> t) & 1u) o |= inner[t];
+		return o;
+	};
+	const uint32_t D = 1u << all.size();
+	std::vector<std::complex<double>> out(static_cast<size_t>(D) * D, 0.0);
+	for (uint32_t i = 0; i < D; ++i)
+		for (uint32_t j = 0; j < D; ++j)
+			if ((i & extra) == (j & extra)) out[static_cast<size_t>(i) * D + j] = M[static_cast<size_t>(old_index(i)) * d + old_index(j)];
+	pos = all;
+	return out;
+}
+
+// the tile bits outside a tensor-core block, in the order that makes up the row (tensor-memory lane)
+// index: first four whose swizzled offsets differ in independent low-four-bit vectors (conflict-free
+// gathers, tc_swizzle), then the rest ascending; packed 4 bits each, row bit r in bits 4r..4r+3
+uint64_t tc_row_order(uint32_t insmask) {
+	std::vector<int> first, rest;
+	uint32_t basis[4] = {0, 0, 0, 0};  // reduced vectors by leading bit
+	for (int b = 0; b < kTcTileQubits; ++b) {
+		if ((insmask >> b) & 1u) continue;
+		uint32_t v = tc_bit_offset(b) & 15u;
+		for (int l = 3; l >= 0; --l)
+			if (((v >> l) & 1u) && basis[l]) v ^= basis[l];
+		if (first.size() < 4 && v) {
+			int l = 3;
+			while (!((v >> l) & 1u)) --l;
+			basis[l] = v;
+			first.push_back(b);
+		} else {
+			rest.push_back(b);
+		}
+	}
+	first.insert(first.end(), rest.begin(), rest.end());
+	uint64_t packed = 0;
+	for (size_t r = 0; r < first.size(); ++r) packed |= static_cast<uint64_t>(first[r]) << (4 * r);
+	return packed;
+}
+
 // host check of one tile operation: inserted positions strictly ascending and below k, the bits it
 // reads or forces inside the inserted set, its matrix entries inside the table
 bool op_in_bounds(const TileOp& op, int k, size_t mats) {
@@ -163,8 +220,12 @@ bool op_in_bounds(const TileOp& op, int k, size_t mats) {
 	if (static_cast<TKind>(op.kind) == TKind::DenseTC) {
 		const uint32_t D = 1u << op.nins;
 		if (k != kTcTileQubits || op.nins < 4 || op.nins > 5 || op.lset != 0 || op.lbit0 != 0 || op.lbit2 != 0 || (op.mat & 1u) ||
-		    (op.lbit1 & 15u) || op.lbit1 + 32 * D * D > kTcMatBudget)
+		    (op.lbit1 & 15u) || op.lbit1 + 32 * D * D > kTcMatBudget || op.gmask != 0)
 			return false;
+		// the row order: every tile bit outside the block exactly once
+		uint32_t rows = 0;
+		for (int r = 0; r < kTcTileQubits - op.nins; ++r) rows |= 1u << ((op.gtbit >> (4 * r)) & 15u);
+		if (rows != (((1u << kTcTileQubits) - 1) & ~insmask) || (op.gtbit >> (4 * (kTcTileQubits - op.nins))) != 0) return false;
 		return op.mat + size_t(4) * D * D <= mats;
 	}
 	if (static_cast<TKind>(op.kind) == TKind::TableDiag)  // every amplitude of the tile, from the table at gtbit
@@ -281,7 +342,10 @@ int run_planned(qcs_handle h, const std::vector<PlannedPass>& passes, int kmax, 
 		tp.nfixed = nf;
 		tp.op_begin = static_cast<uint32_t>(ops.size());
 		uint32_t tc_slot = 0;  // bytes of resident block matrices used in this pass
-		const bool tc_pass = sizeof(T) == 4 && h->tensor_cores && tp.k == kTcTileQubits && L >= 5 && tp.k - L <= 8;
+		// a tensor-core pass: FP32, a 12-qubit tile, and nothing but fused blocks (smaller ones are padded
+		// to 4 qubits); every operation of it runs on the tensor cores
+		bool tc_pass = sizeof(T) == 4 && h->tensor_cores && tp.k == kTcTileQubits && L >= 5 && tp.k - L <= 8 && !pp.gates.empty();
+		for (const CompiledGate& c : pp.gates) tc_pass = tc_pass && c.kind == GKind::Block && !c.block_q.empty();
 		for (const CompiledGate& c : pp.gates) {
 			TileOp op;
 			std::memset(&op, 0, sizeof(op));
@@ -345,16 +409,29 @@ int run_planned(qcs_handle h, const std::vector<PlannedPass>& passes, int kmax, 
 				op.pad[2] = c.row_inverse ? 1 : 0;
 				op.pad[3] = static_cast<uint8_t>(rowM);
 				op.mat = row_tab;
-			} else if (c.kind == GKind::Block && tc_pass && c.block_q.size() >= 4 &&
-			           tc_slot + 32u * (1u << (2 * c.block_q.size())) <= kTcMatBudget) {
+			} else if (c.kind == GKind::Block && tc_pass) {
 				if constexpr (sizeof(T) == 4) {
+					std::vector<int> pos;
+					for (uint32_t q : c.block_q) pos.push_back(lpos[q]);
+					std::vector<std::complex<double>> M = c.block_m;
+					if (pos.size() < 4) M = pad_block(pos, M, tp.k);
+					const uint32_t K = static_cast<uint32_t>(pos.size());
+					if (tc_slot + 32u * (1u << (2 * K)) > kTcMatBudget) {
+						h->err = "apply gates: internal error (tensor-core pass over its matrix budget)";
+						return QCS_CUDA_ERROR;
+					}
 					op.kind = static_cast<uint8_t>(TKind::DenseTC);
-					for (uint32_t q : c.block_q) ins.push_back(lpos[q]);
+					uint32_t insmask = 0;
+					for (int b : pos) {
+						ins.push_back(b);
+						insmask |= 1u << b;
+					}
+					op.gtbit = tc_row_order(insmask);
 					if (mats.size() & 1) mats.push_back(mk_host<T>(0.0, 0.0));
 					op.mat = static_cast<uint32_t>(mats.size());
-					push_block_tc(mats, c.block_m, 1u << c.block_q.size());
+					push_block_tc(mats, M, 1u << K);
 					op.lbit1 = tc_slot;
-					tc_slot += 32u * (1u << (2 * c.block_q.size()));
+					tc_slot += 32u * (1u << (2 * K));
 					tp.dense = 2;
 				}
 			} else if (c.kind == GKind::TableDiag) {
@@ -420,7 +497,7 @@ int run_planned(qcs_handle h, const std::vector<PlannedPass>& passes, int kmax, 
 			return QCS_CUDA_ERROR;
 		}
 		for (uint32_t i = tp.op_begin; i < tp.op_begin + tp.op_count; ++i)
-			if (!op_in_bounds(ops[i], tp.k, mats.size()) || (tp.dense == 2 && static_cast<TKind>(ops[i].kind) == TKind::TableDiag) ||
+			if (!op_in_bounds(ops[i], tp.k, mats.size()) || (tp.dense == 2) != (static_cast<TKind>(ops[i].kind) == TKind::DenseTC) ||
 			    (static_cast<TKind>(ops[i].kind) == TKind::PhaseRow && ops[i].pad[4] &&
 			     (ops[i].pad[3] != bb->roots_M || ops[i].gtbit != reinterpret_cast<uint64_t>(bb->d_roots)))) {
 				h->err = "apply gates: internal error (tile operation out of range)";

@@ -152,6 +152,13 @@ cudaError_t inner_product_f64b(const cplx_t<T>* a, const double2* b, uint64_t N,
 template <typename T>
 cudaError_t sample(const cplx_t<T>* s, uint64_t N, const double* probs_host, size_t nshots, int mode,
                    uint64_t fallback, Scratch& sc, int sms, cudaStream_t st, uint64_t* out_host);
+// registers of at most 2048 amplitudes: one measurement in one launch (kind 0: Measure with collapse onto
+// the sampled value of the `mask` qubits; 1: MeasureAll; 2: MeasureNoCollapse); *out_host = the sampled
+// state, `fallback` when the running sum never reaches prob
+constexpr uint64_t kSmallMeasure = 2048;
+template <typename T>
+cudaError_t measure_small(cplx_t<T>* s, uint64_t N, double prob, uint64_t mask, int kind, uint64_t fallback, Scratch& sc,
+                          cudaStream_t st, uint64_t* out_host);
 template <typename T>
 cudaError_t convert_from_f64(cplx_t<T>* dst, const double2* src, uint64_t N, int sms, cudaStream_t st);
 template <typename T>

@@ -215,7 +215,8 @@ std::vector<std::vector<size_t>> pack_blocks(const std::vector<FusedBlock>& bloc
 	for (size_t i = 0; i < blocks.size(); ++i) {
 		for (uint32_t q : blocks[i].qubits) mask[i] |= 1ULL << q;
 		if (blocks[i].qubits.empty()) placed[i] = 1;
-		if (tc_budget && blocks[i].qubits.size() >= 4) tcb[i] = 32u << (2 * blocks[i].qubits.size());
+		// tensor-core passes widen smaller blocks to 4 qubits
+		if (tc_budget && !blocks[i].qubits.empty()) tcb[i] = 32u << (2 * std::max<size_t>(4, blocks[i].qubits.size()));
 	}
 	const uint64_t low = (L0 >= 64) ? ~0ULL : ((1ULL << L0) - 1);
 	while (true) {

@@ -33,8 +33,8 @@ std::vector<FusedBlock> fuse(const std::vector<CompiledGate>& gates, const Fusio
 // packs blocks into shared-memory passes of at most kmax tile qubits (qubits below L0 always in the
 // tile): each pass takes, in order, every block that fits and shares no qubit with an earlier block
 // still waiting (blocks on disjoint qubits commute), looking at most `window` blocks ahead.  With
-// tc_budget > 0, blocks of 4 and 5 qubits also draw 32 x 4^m bytes of resident matrices from that
-// budget.  Blocks without qubits (global factors) take no pass.  Returns the block indices of each
+// tc_budget > 0 (tensor-core passes), every block also draws 32 x 4^max(m, 4) bytes of resident
+// matrices from that budget.  Blocks without qubits (global factors) take no pass.  Returns the block indices of each
 // pass, each in the original order.
 std::vector<std::vector<size_t>> pack_blocks(const std::vector<FusedBlock>& blocks, int kmax, int L0, uint32_t tc_budget,
                                              size_t window = 64);

@@ -4,6 +4,8 @@
 // sums in a fixed order, then a single block folds the per-block partials.  Probabilities are
 // computed as re*re + im*im in FP64 with explicit round-to-nearest operations (no contraction),
 // so every path sees the same |a_i|^2 values.
+#include <cstring>
+
 #include "engine.cuh"
 
 #include <vector>
@@ -241,6 +243,60 @@ __global__ void k_sample(const cplx_t<T>* __restrict__ s, uint64_t N, const doub
 	out[k] = (i == N) ? fallback : i;
 }
 
+// one measurement of a register of at most kChunk amplitudes in one launch of one block: the sampled
+// state by the reference's running sum (the semantics of find_first with a single chunk), then
+//   kind 0 (Measure):          collapse onto the sampled value of the masked qubits, renormalised;
+//   kind 1 (MeasureAll):       the basis state sampled (all amplitudes rewritten);
+//   kind 2 (MeasureNoCollapse): nothing written.
+// out[0] = the sampled state (fallback when the running sum never reaches prob)
+template <typename T>
+__global__ void __launch_bounds__(kRedThreads) k_measure_small(cplx_t<T>* __restrict__ s, uint64_t N, double prob, uint64_t mask, int kind,
+                                                             uint64_t fallback, unsigned long long* __restrict__ out) {
+	__shared__ double sh[kRedThreads];
+	__shared__ unsigned long long picked;
+	if (threadIdx.x == 0) {
+		double acc = 0;
+		uint64_t st = fallback;
+		for (uint64_t i = 0; i < N; ++i) {
+			acc = __dadd_rn(acc, probd<T>(s[i]));
+			if (prob <= acc) {
+				st = i;
+				break;
+			}
+		}
+		picked = st;
+		out[0] = st;
+	}
+	__syncthreads();
+	const uint64_t st = picked;
+	if (kind == 2) return;
+	if (kind == 1) {
+		for (uint64_t i = threadIdx.x; i < N; i += blockDim.x) {
+			cplx_t<T> v;
+			v.x = static_cast<T>(i == st ? 1 : 0);
+			v.y = static_cast<T>(0);
+			s[i] = v;
+		}
+		return;
+	}
+	const uint64_t value = st & mask;
+	double acc = 0;
+	for (uint64_t i = threadIdx.x; i < N; i += blockDim.x)
+		if ((i & mask) == value) {
+			const double x = static_cast<double>(s[i].x), y = static_cast<double>(s[i].y);
+			acc = fma(y, y, fma(x, x, acc));
+		}
+	const double total = block_sum(acc, sh);
+	const double f = 1.0 / sqrt(total);
+	for (uint64_t i = threadIdx.x; i < N; i += blockDim.x) {
+		const double g = ((i & mask) == value) ? f : 0.0;
+		cplx_t<T> v = s[i];
+		v.x = static_cast<T>(static_cast<double>(v.x) * g);
+		v.y = static_cast<T>(static_cast<double>(v.y) * g);
+		s[i] = v;
+	}
+}
+
 template <typename T>
 __global__ void k_from_f64(cplx_t<T>* __restrict__ d, const double2* __restrict__ s, uint64_t N) {
 	const uint64_t stride = static_cast<uint64_t>(gridDim.x) * blockDim.x;
@@ -445,6 +501,23 @@ cudaError_t sample(const cplx_t<T>* s, uint64_t N, const double* probs_host, siz
 }
 
 template <typename T>
+cudaError_t measure_small(cplx_t<T>* s, uint64_t N, double prob, uint64_t mask, int kind, uint64_t fallback, Scratch& sc,
+                          cudaStream_t st, uint64_t* out_host) {
+	if (N > kChunk) return cudaErrorInvalidValue;
+	cudaError_t e = ensure_red(sc, 4);
+	if (e == cudaSuccess) e = ensure_pinned(sc, 4);
+	if (e != cudaSuccess) return e;
+	auto* dv = reinterpret_cast<unsigned long long*>(sc.d_red);
+	k_measure_small<T><<<1, kRedThreads, 0, st>>>(s, N, prob, mask, kind, fallback, dv);
+	note_launches(1);
+	if ((e = cudaGetLastError()) != cudaSuccess) return e;
+	if ((e = cudaMemcpyAsync(sc.h_pinned, dv, sizeof(unsigned long long), cudaMemcpyDeviceToHost, st)) != cudaSuccess) return e;
+	if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return e;
+	std::memcpy(out_host, sc.h_pinned, sizeof(uint64_t));
+	return cudaSuccess;
+}
+
+template <typename T>
 cudaError_t convert_from_f64(cplx_t<T>* dst, const double2* src, uint64_t N, int sms, cudaStream_t st) {
 	k_from_f64<T><<<grid_for(N, 256, sms), 256, 0, st>>>(dst, src, N);
 	note_launches(1);
@@ -476,6 +549,7 @@ cudaError_t launch_operator_matrix(const double2* M, const cplx_t<T>* in, cplx_t
 	template cudaError_t inner_product<T>(const cplx_t<T>*, const cplx_t<T>*, uint64_t, Scratch&, int, cudaStream_t, double*); \
 	template cudaError_t inner_product_f64b<T>(const cplx_t<T>*, const double2*, uint64_t, Scratch&, int, cudaStream_t, double*); \
 	template cudaError_t sample<T>(const cplx_t<T>*, uint64_t, const double*, size_t, int, uint64_t, Scratch&, int, cudaStream_t, uint64_t*); \
+	template cudaError_t measure_small<T>(cplx_t<T>*, uint64_t, double, uint64_t, int, uint64_t, Scratch&, cudaStream_t, uint64_t*); \
 	template cudaError_t convert_from_f64<T>(cplx_t<T>*, const double2*, uint64_t, int, cudaStream_t);              \
 	template cudaError_t convert_to_f64<T>(double2*, const cplx_t<T>*, uint64_t, int, cudaStream_t);                \
 	template cudaError_t launch_operator_matrix<T>(const double2*, const cplx_t<T>*, cplx_t<T>*, uint64_t, int, cudaStream_t);

@@ -26,6 +26,18 @@ enum class TKind : uint8_t { Ctrl1q = 0, Swap = 1, Dense2 = 2, Dense3 = 3, Globa
 constexpr int kTcTileQubits = 12;
 constexpr uint32_t kTcMatBudget = 65536;  // two 5-qubit blocks, or eight 4-qubit blocks
 
+// A tensor-core pass keeps its tile in shared memory under an XOR swizzle: amplitude x of the tile sits
+// at x ^ S(x >> 4), S linear over GF(2) with the 4-bit vectors tc_swizzle(b) for tile bits b = 4..11.
+// Bits 0..3 add the unit vectors, and the twelve vectors are distinct and nonzero and avoid
+// {0011, 1100, 1111}, which meets every 3-dimensional subspace of GF(2)^4; so any seven of them span
+// GF(2)^4.  For a block on 4 or 5 tile bits, four of the remaining bits therefore change the low four
+// bits of the address independently: 16 lanes reading 8-byte amplitudes along them use 16 bank pairs.
+__host__ __device__ constexpr uint32_t tc_swizzle(int b) {
+	return b < 4 ? 0u : static_cast<uint32_t>((0xEDBA9765ULL >> (4 * (b - 4))) & 15u);
+}
+// swizzled offset (in amplitudes) of tile bit b: the address of amplitude x is the XOR over its set bits
+__host__ __device__ constexpr uint32_t tc_bit_offset(int b) { return (1u << b) ^ tc_swizzle(b); }
+
 // one gate inside a pass, in tile-local bit positions
 struct TileOp {
 	uint8_t kind;      // TKind

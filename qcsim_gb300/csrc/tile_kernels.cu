@@ -414,24 +414,32 @@ __global__ void __launch_bounds__(THREADS) k_tile(cplx_t<T>* __restrict__ s, Til
 	}
 }
 
-// ---- tensor-core passes (FP32 registers, fused 4- and 5-qubit blocks) ----
+// ---- tensor-core passes (FP32 registers, fused blocks on 4 or 5 tile qubits) ----
 //
-// A block of K qubits (D = 2^K) acts on the tile's C = 2^12 / D "columns" (assignments of the other
-// tile qubits).  As a real product: out (C x 2D) = in (C x 2D) * B (2D x 2D), in[c][2j + p] = part p of
+// A block of K qubits (D = 2^K) acts on the tile's 2^12 / D "columns" (assignments of the other tile
+// qubits).  As a real product: out (C x 2D) = in (C x 2D) * B (2D x 2D), in[c][2j + p] = part p of
 // amplitude j of column c, B[2j][2i] = Re M[i][j], B[2j + 1][2i] = -Im M[i][j], B[2j][2i + 1] = Im M[i][j],
-// B[2j + 1][2i + 1] = Re M[i][j].  Columns are the MMA's M dimension (tiles of 128 rows), 2D its N and
-// K.  3xTF32: each operand is split into TF32 hi + lo parts and out = in_hi B_hi + in_hi B_lo + in_lo B_hi,
+// B[2j + 1][2i + 1] = Re M[i][j].  Columns are the MMA's M dimension (tiles of 128 rows), 2D its N and K.
+// 3xTF32: each operand is split into TF32 hi + lo parts and out = in_hi B_hi + in_hi B_lo + in_lo B_hi,
 // accumulated in FP32 in tensor memory.
 //
-// Shared memory: the 32 KiB tile, the A operand (hi and lo splits) and the pass's block matrices (hi
-// and lo, kTcMatBudget bytes), loaded once per CTA.
+// The A operand goes to tensor memory, not shared memory: each thread gathers the amplitudes of one
+// column (one tensor-memory lane) from the swizzled tile, splits them and writes them with tcgen05.st;
+// the MMAs read A from tensor memory and B (the pass's block matrices, resident in shared memory).
+// Tensor memory per CTA: accumulators in columns [0, 128), A (hi and lo) in [128, 256).  Which tile
+// bits make up the row (lane) index is chosen on the host per block (op.gtbit: 4-bit tile positions,
+// row bit r in bits 4r..4r+3), so that the lanes of a half-warp read 16 different bank pairs.
+// Shared memory: the 32 KiB tile and kTcMatBudget bytes of block matrices: two CTAs per SM, one
+// computing while the other's MMAs run.
+constexpr int kTcThreads = 256;
 constexpr uint32_t kTcTileBytes = (1u << kTcTileQubits) * sizeof(float2);
-constexpr uint32_t kTcLboA = 144;     // A operand: a row's core matrices fall in different bank groups
-constexpr uint32_t kTcABytes = 36864;  // one split of A: 16 row groups x 16 core matrices x 144 bytes
-constexpr uint32_t kTcSmem = kTcTileBytes + 2 * kTcABytes + kTcMatBudget;  // plus the pass's operations
-constexpr uint32_t kTcSmemLimit = 216 * 1024;                                 // dynamic, with 9 KB static beside it
-constexpr uint32_t kTcTmemCols = 128;  // per M tile: kdim accumulator columns + kdim hi*lo columns
+constexpr uint32_t kTcSmem = kTcTileBytes + kTcMatBudget;  // plus the pass's operations
+constexpr uint32_t kTcSmemLimit = 100 * 1024;               // dynamic; two CTAs per SM with the static tables
+constexpr uint32_t kTcTmemCols = 256;
+constexpr uint32_t kTcAcol = 128;  // first tensor-memory column of the A operands
 constexpr uint32_t kTcWaitTries = 1u << 22;
+constexpr int kTcLoads = (1 << kTcTileQubits) / kTcThreads;  // 16 amplitudes per thread and tile
+static_assert(kTcThreads == 256 && kTcTileQubits == 12, "tile index = thread + 256 i");
 
 __device__ __forceinline__ float tf32_rna(float x) {
 	uint32_t r;
@@ -439,108 +447,79 @@ __device__ __forceinline__ float tf32_rna(float x) {
 	return __uint_as_float(r);
 }
 
-// the K block positions of a DenseTC op, ascending
-template <int K> struct BlockBits {
-	uint32_t pos[K];
-	__device__ __forceinline__ explicit BlockBits(uint64_t ins) {
-#pragma unroll
-		for (int t = 0; t < K; ++t) pos[t] = static_cast<uint32_t>((ins >> (8 * t)) & 0xffu);
-	}
-	// tile index -> column (the index without the block bits)
-	__device__ __forceinline__ uint32_t column(uint32_t x) const {
-#pragma unroll
-		for (int t = K - 1; t >= 0; --t) x = ((x >> (pos[t] + 1)) << pos[t]) | (x & ((1u << pos[t]) - 1));
-		return x;
-	}
-	// tile index -> block index j
-	__device__ __forceinline__ uint32_t index(uint32_t x) const {
-		uint32_t j = 0;
-#pragma unroll
-		for (int t = 0; t < K; ++t) j |= ((x >> pos[t]) & 1u) << t;
-		return j;
-	}
-	// (column, block index) -> tile index
-	__device__ __forceinline__ uint32_t place(uint32_t c, uint32_t j) const {
-#pragma unroll
-		for (int t = 0; t < K; ++t) c = ((c >> pos[t]) << (pos[t] + 1)) | (c & ((1u << pos[t]) - 1)) | (((j >> t) & 1u) << pos[t]);
-		return c;
-	}
-	__device__ __forceinline__ uint32_t low_count() const {
-		uint32_t n = 0;
-#pragma unroll
-		for (int t = 0; t < K; ++t) n += pos[t] < 5 ? 1u : 0u;
-		return n;
-	}
-};
+// swizzled offset of tile index x (XOR of the offsets of its set bits)
+__host__ __device__ constexpr uint32_t tc_offset(uint32_t x) {
+	uint32_t o = 0;
+	for (int b = 0; b < kTcTileQubits; ++b)
+		if ((x >> b) & 1u) o ^= tc_bit_offset(b);
+	return o;
+}
 
-// applies one DenseTC op of K qubits to the tile; false when the MMA completion wait ran out.
-// Every index map of the op (tile index -> A-operand byte offset, tile index -> staging slot) is a sum
-// of one weight per set tile bit, so a thread's eight elements (tile index = thread + 512 b) cost one
-// 9-term sum for the thread's bits and three weights for b.
+// one block of K = 4 or 5 qubits on the tile: gather and split into tensor memory, 3xTF32 MMAs, then the
+// outputs back into the tile.  false when the MMA completion wait ran out.
+//   K = 5: one M tile (128 columns of 32 amplitudes); warp w: lanes 32 (w % 4) + 0..31, amplitudes
+//          j in [16 (w / 4), 16 (w / 4) + 16)
+//   K = 4: two M tiles (256 columns of 16 amplitudes); warp w: M tile w / 4, lanes 32 (w % 4) + 0..31,
+//          all 16 amplitudes
 template <int K>
-__device__ bool tile_block_tc(float2* sm, uint64_t ins, unsigned char* sA, const unsigned char* sBop, uint32_t tmem, uint64_t* mbar,
-                              uint32_t& phase) {
+__device__ bool tc_block(float2* sm, const TileOp& op, const unsigned char* sBop, uint32_t tmem, uint64_t* mbar, uint32_t& phase) {
 	constexpr uint32_t D = 1u << K, kdim = 2 * D;
-	constexpr uint32_t sbo_a = (kdim / 4) * kTcLboA, sbo_b = (kdim / 4) * 128;
-	constexpr uint32_t cols = (1u << kTcTileQubits) >> K;  // 128 (K = 5) or 256 (K = 4)
-	constexpr uint32_t mt_bytes = 16 * sbo_a;                // one 128-row M tile of one split
-	constexpr uint32_t kTidBits = 9;                          // kTileThreads = 2^9
-	static_assert(kTileThreads == (1 << kTidBits) && kTcTileQubits == kTidBits + 3, "tile index = thread + 512 b");
-	const BlockBits<K> bb(ins);
-	// per tile bit: byte offset in one A split (a block bit is bit t of j, the K index is 2j + part; a
-	// column bit is bit r of the column: rows within a core matrix, row groups, then the M tile) and
-	// slot in the staging area (slot = j (cols + 1) + column)
-	uint32_t wa[kTcTileQubits], ws[kTcTileQubits];
-	{
-		uint32_t t = 0;
+	constexpr uint32_t sbo_b = (kdim / 4) * 128;
+	const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
+	const uint32_t quad = warp & 3u, h = warp >> 2;
+	const uint32_t m = 32u * quad + lane;  // row in the M tile
+	// swizzled offsets of the block bits and of this thread's row
+	uint32_t bw[K];
 #pragma unroll
-		for (uint32_t i = 0; i < kTcTileQubits; ++i) {
-			if (t < K && bb.pos[t == K ? 0 : t] == i) {
-				wa[i] = t == 0 ? 8u : (kTcLboA << (t - 1));
-				ws[i] = (cols + 1) << t;
-				++t;
-			} else {
-				const uint32_t r = i - t;
-				wa[i] = r < 3 ? (16u << r) : (r < 7 ? (sbo_a << (r - 3)) : mt_bytes);
-				ws[i] = 1u << r;
-			}
+	for (int t = 0; t < K; ++t) bw[t] = tc_bit_offset(static_cast<int>((op.ins >> (8 * t)) & 0xffu));
+	uint32_t rb = 0;
+#pragma unroll
+	for (int r = 0; r < 7; ++r)
+		if ((m >> r) & 1u) rb ^= tc_bit_offset(static_cast<int>((op.gtbit >> (4 * r)) & 15u));
+	if (K == 4 && h) rb ^= tc_bit_offset(static_cast<int>((op.gtbit >> 28) & 15u));  // the M tile's row bit
+	if (K == 5 && h) rb ^= bw[K - 1];                                                  // j = 16 h + jj
+	// tensor-memory columns of this thread's A values and accumulators
+	const uint32_t lanes = (32u * quad) << 16;
+	const uint32_t a_hi = K == 5 ? kTcAcol + 32u * h : kTcAcol + 64u * h;
+	const uint32_t a_lo = K == 5 ? kTcAcol + 64u + 32u * h : kTcAcol + 64u * h + 32u;
+	const uint32_t acc = K == 5 ? 32u * h : 64u * h;
+	const uint32_t hilo = K == 5 ? 64u + 32u * h : 64u * h + 32u;
+#pragma unroll
+	for (uint32_t c8 = 0; c8 < 2; ++c8) {
+		const uint32_t base = rb ^ (c8 ? bw[3] : 0u);
+		float hi[16], lo[16];
+#pragma unroll
+		for (uint32_t u = 0; u < 8; ++u) {
+			const uint32_t off = base ^ ((u & 1u) ? bw[0] : 0u) ^ ((u & 2u) ? bw[1] : 0u) ^ ((u & 4u) ? bw[2] : 0u);
+			const float2 v = sm[off];
+			const float hx = tf32_rna(v.x), hy = tf32_rna(v.y);
+			hi[2 * u] = hx;
+			hi[2 * u + 1] = hy;
+			lo[2 * u] = tf32_rna(v.x - hx);
+			lo[2 * u + 1] = tf32_rna(v.y - hy);
 		}
+		tc::tmem_st16(tmem + lanes + a_hi + 16u * c8, hi);
+		tc::tmem_st16(tmem + lanes + a_lo + 16u * c8, lo);
 	}
-	uint32_t a_tid = 0, s_tid = 0;
-#pragma unroll
-	for (uint32_t i = 0; i < kTidBits; ++i)
-		if ((threadIdx.x >> i) & 1u) {
-			a_tid += wa[i];
-			s_tid += ws[i];
-		}
-	// gather in tile order (conflict-free reads) into the A operand, split into TF32 hi and lo
-#pragma unroll
-	for (uint32_t b = 0; b < 8; ++b) {
-		const float2 v = sm[threadIdx.x + (b << kTidBits)];
-		const uint32_t off = a_tid + ((b & 1u) ? wa[9] : 0u) + ((b & 2u) ? wa[10] : 0u) + ((b & 4u) ? wa[11] : 0u);
-		const float hx = tf32_rna(v.x), hy = tf32_rna(v.y);
-		*reinterpret_cast<float2*>(sA + off) = make_float2(hx, hy);
-		*reinterpret_cast<float2*>(sA + kTcABytes + off) = make_float2(tf32_rna(v.x - hx), tf32_rna(v.y - hy));
-	}
-	tc::fence_proxy_async();
+	tc::tmem_wait_st();
 	tc::fence_before_sync();
 	__syncthreads();
-	tc::fence_after_sync();
 	if (threadIdx.x == 0) {
-		constexpr uint32_t idesc = tc::idesc_tf32(128, kdim), idesc2 = tc::idesc_tf32(128, 2 * kdim);
-		const uint32_t a_hi = tc::smem_addr(sA), b_hi = tc::smem_addr(sBop);
-		// descriptors of k-step 0; each k-step advances the start address (16-byte units, low bits)
-		const uint64_t ah0 = tc::smem_desc(a_hi, kTcLboA, sbo_a), al0 = tc::smem_desc(a_hi + kTcABytes, kTcLboA, sbo_a);
-		const uint64_t bh0 = tc::smem_desc(b_hi, 128, sbo_b);
+		tc::fence_after_sync();
+		const uint64_t bh0 = tc::smem_desc(tc::smem_addr(sBop), 128, sbo_b);
+		constexpr uint32_t nmt = K == 5 ? 1u : 2u;
+		constexpr uint32_t idesc2 = tc::idesc_tf32(128, 2 * kdim), idesc1 = tc::idesc_tf32(128, kdim);
 #pragma unroll
-		for (uint32_t mt = 0; mt < cols / 128; ++mt) {
+		for (uint32_t mt = 0; mt < nmt; ++mt) {
+			const uint32_t d = tmem + mt * 2u * kdim;
+			const uint32_t ah = tmem + kTcAcol + mt * 2u * kdim, al = ah + kdim;
 #pragma unroll
 			for (uint32_t ks = 0; ks < kdim / 8; ++ks) {
-				const uint64_t da = (mt * mt_bytes + ks * 2 * kTcLboA) >> 4, db = (ks * 2 * 128) >> 4;
+				const uint64_t db = (ks * 2 * 128) >> 4;  // a k-step is two core matrices of B along K
 				// B_lo directly follows B_hi: one N = 2 kdim product gives hi*hi in the first kdim columns
 				// and hi*lo in the next kdim; lo*hi accumulates onto the first
-				tc::mma_tf32(tmem + mt * 2 * kdim, ah0 + da, bh0 + db, idesc2, ks > 0 ? 1u : 0u);
-				tc::mma_tf32(tmem + mt * 2 * kdim, al0 + da, bh0 + db, idesc, 1u);
+				tc::mma_tf32_ta(d, ah + 8u * ks, bh0 + db, idesc2, ks > 0 ? 1u : 0u);
+				tc::mma_tf32_ta(d, al + 8u * ks, bh0 + db, idesc1, 1u);
 			}
 		}
 		tc::mma_commit(mbar);
@@ -548,45 +527,24 @@ __device__ bool tile_block_tc(float2* sm, uint64_t ins, unsigned char* sA, const
 	const bool ok = tc::mbar_wait(mbar, phase, kTcWaitTries);
 	phase ^= 1u;
 	tc::fence_after_sync();
-	// warp w reads tensor-memory lanes 32 (w % 4) + 0..31 (M-tile rows = columns), 16 accumulator
-	// columns (8 complex outputs i0..i0 + 7) and the matching 16 hi*lo columns kdim further on
-	const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
-	const uint32_t quad = warp & 3u, cc = warp >> 2;
-	const uint32_t mt = (16u * cc) / kdim, within = (16u * cc) % kdim, i0 = within / 2;  // i0: a multiple of 8
-	float v[16], w[16];
-	const uint32_t tcol = tmem + ((32u * quad) << 16) + mt * 2 * kdim + within;
-	tc::tmem_ld16(tcol, v);
-	tc::tmem_ld16(tcol + kdim, w);
 #pragma unroll
-	for (int q = 0; q < 16; ++q) v[q] += w[q];
-	const uint32_t c = mt * 128u + 32u * quad + lane;
-	// blocks on three or more of the five lowest tile bits: outputs go through a padded staging area
-	// (the A operand is free now) and back to the tile in tile order; otherwise straight to the tile
-	const bool staged = bb.low_count() >= 3;
-	if (!staged) {
-		const uint32_t x0 = bb.place(c, i0);
-		const uint32_t p0 = 1u << bb.pos[0], p1 = 1u << bb.pos[1], p2 = 1u << bb.pos[2];
+	for (uint32_t c8 = 0; c8 < 2; ++c8) {
+		float v[16], w[16];
+		tc::tmem_ld16(tmem + lanes + acc + 16u * c8, v);
+		tc::tmem_ld16(tmem + lanes + hilo + 16u * c8, w);
+		const uint32_t base = rb ^ (c8 ? bw[3] : 0u);
 #pragma unroll
-		for (uint32_t t = 0; t < 8; ++t)
-			sm[x0 + ((t & 1u) ? p0 : 0u) + ((t & 2u) ? p1 : 0u) + ((t & 4u) ? p2 : 0u)] = make_float2(v[2 * t], v[2 * t + 1]);
-	} else {
-		float2* stage = reinterpret_cast<float2*>(sA);
-#pragma unroll
-		for (uint32_t t = 0; t < 8; ++t) stage[(i0 + t) * (cols + 1) + c] = make_float2(v[2 * t], v[2 * t + 1]);
+		for (uint32_t u = 0; u < 8; ++u) {
+			const uint32_t off = base ^ ((u & 1u) ? bw[0] : 0u) ^ ((u & 2u) ? bw[1] : 0u) ^ ((u & 4u) ? bw[2] : 0u);
+			sm[off] = make_float2(v[2 * u] + w[2 * u], v[2 * u + 1] + w[2 * u + 1]);
+		}
 	}
 	tc::fence_before_sync();
-	if (staged) {
-		__syncthreads();
-		const float2* stage = reinterpret_cast<const float2*>(sA);
-#pragma unroll
-		for (uint32_t b = 0; b < 8; ++b)
-			sm[threadIdx.x + (b << kTidBits)] = stage[s_tid + ((b & 1u) ? ws[9] : 0u) + ((b & 2u) ? ws[10] : 0u) + ((b & 4u) ? ws[11] : 0u)];
-	}
 	return ok;
 }
 
-__global__ void __launch_bounds__(kTileThreads, 1) k_tile_tc(float2* __restrict__ s, TilePass p, const TileOp* __restrict__ ops,
-                                                              const float2* __restrict__ mats, uint64_t ntiles, int* err) {
+__global__ void __launch_bounds__(kTcThreads, 2) k_tile_tc(float2* __restrict__ s, TilePass p, const TileOp* __restrict__ ops,
+                                                           const float2* __restrict__ mats, uint64_t ntiles, int* err) {
 	extern __shared__ __align__(1024) unsigned char smraw[];
 	__shared__ uint64_t highoff[1 << kMaxHigh];
 	__shared__ uint64_t fixtab[kFixChunks][256];
@@ -594,8 +552,7 @@ __global__ void __launch_bounds__(kTileThreads, 1) k_tile_tc(float2* __restrict_
 	__shared__ uint32_t tmem_slot;
 	__shared__ int stop;
 	float2* sm = reinterpret_cast<float2*>(smraw);
-	unsigned char* sA = smraw + kTcTileBytes;
-	unsigned char* sB = sA + 2 * kTcABytes;
+	unsigned char* sB = smraw + kTcTileBytes;
 	// the pass's operations, copied once (behind the block matrices)
 	TileOp* sops = reinterpret_cast<TileOp*>(sB + kTcMatBudget);
 	for (uint32_t i = threadIdx.x; i < p.op_count; i += blockDim.x) sops[i] = ops[p.op_begin + i];
@@ -603,11 +560,11 @@ __global__ void __launch_bounds__(kTileThreads, 1) k_tile_tc(float2* __restrict_
 	const uint32_t warp = threadIdx.x >> 5;
 	const uint32_t lowmask = (1u << p.L) - 1;
 	const int nh = p.k - p.L;
-	for (uint32_t h = threadIdx.x; h < (1u << nh); h += blockDim.x) {
+	for (uint32_t hh = threadIdx.x; hh < (1u << nh); hh += blockDim.x) {
 		uint64_t off = 0;
 		for (int b = 0; b < nh; ++b)
-			if ((h >> b) & 1u) off |= 1ULL << p.high[b];
-		highoff[h] = off;
+			if ((hh >> b) & 1u) off |= 1ULL << p.high[b];
+		highoff[hh] = off;
 	}
 	if (warp == 0) tc::tmem_alloc<kTcTmemCols>(&tmem_slot);
 	if (threadIdx.x == 0) {
@@ -617,7 +574,6 @@ __global__ void __launch_bounds__(kTileThreads, 1) k_tile_tc(float2* __restrict_
 	// the pass's block matrices stay resident for every tile
 	for (uint32_t oi = 0; oi < p.op_count; ++oi) {
 		const TileOp& op = ops[p.op_begin + oi];
-		if (static_cast<TKind>(op.kind) != TKind::DenseTC) continue;
 		const uint32_t bytes = 32u << (2 * op.nins);
 		const uint4* src = reinterpret_cast<const uint4*>(mats + op.mat);
 		uint4* dst = reinterpret_cast<uint4*>(sB + op.lbit1);
@@ -628,59 +584,52 @@ __global__ void __launch_bounds__(kTileThreads, 1) k_tile_tc(float2* __restrict_
 	__syncthreads();
 	tc::fence_after_sync();
 	const uint32_t tmem = tmem_slot;
-	constexpr uint32_t kAmps = 1u << kTcTileQubits;
-	constexpr int kBatch = kAmps / kTileThreads;  // 8 loads in flight per thread
 	uint32_t mma_phase = 0;
-	auto tile_base = [&](uint64_t tile) { return fixed_base(fixtab, tile); };
-	// the next tile's amplitudes are loaded into registers while the current tile is processed
-	float2 pre[kBatch];
+	// this thread's amplitudes of a tile: x = thread + 256 i; swizzled offsets tid_off ^ tc_offset(256 i)
+	const uint32_t tid_off = tc_offset(threadIdx.x);
+	float2 pre[kTcLoads];
 	if (blockIdx.x < ntiles) {
-		const uint64_t b0 = tile_base(blockIdx.x);
+		const uint64_t b0 = fixed_base(fixtab, blockIdx.x);
 #pragma unroll
-		for (int b = 0; b < kBatch; ++b) {
-			const uint32_t j = threadIdx.x + b * kTileThreads;
-			pre[b] = s[b0 | highoff[j >> p.L] | (j & lowmask)];
+		for (int i = 0; i < kTcLoads; ++i) {
+			const uint32_t x = threadIdx.x + kTcThreads * i;
+			pre[i] = s[b0 | highoff[x >> p.L] | (x & lowmask)];
 		}
 	}
 	for (uint64_t tile = blockIdx.x; tile < ntiles && !stop; tile += gridDim.x) {
-		const uint64_t base = tile_base(tile);
+		const uint64_t base = fixed_base(fixtab, tile);
 #pragma unroll
-		for (int b = 0; b < kBatch; ++b) sm[threadIdx.x + b * kTileThreads] = pre[b];
+		for (int i = 0; i < kTcLoads; ++i) sm[tid_off ^ tc_offset(kTcThreads * i)] = pre[i];
 		const uint64_t next = tile + gridDim.x;
 		if (next < ntiles) {
-			const uint64_t nb = tile_base(next);
+			const uint64_t nb = fixed_base(fixtab, next);
 #pragma unroll
-			for (int b = 0; b < kBatch; ++b) {
-				const uint32_t j = threadIdx.x + b * kTileThreads;
-				pre[b] = s[nb | highoff[j >> p.L] | (j & lowmask)];
+			for (int i = 0; i < kTcLoads; ++i) {
+				const uint32_t x = threadIdx.x + kTcThreads * i;
+				pre[i] = s[nb | highoff[x >> p.L] | (x & lowmask)];
 			}
 		}
 		__syncthreads();
 		for (uint32_t oi = 0; oi < p.op_count; ++oi) {
-			const TileOp op = sops[oi];
-			if ((base & op.gmask) != op.gmask) continue;
-			if (static_cast<TKind>(op.kind) == TKind::DenseTC) {
-				const bool ok = op.nins == 5 ? tile_block_tc<5>(sm, op.ins, sA, sB + op.lbit1, tmem, &mbar_mma, mma_phase)
-				                             : tile_block_tc<4>(sm, op.ins, sA, sB + op.lbit1, tmem, &mbar_mma, mma_phase);
-				if (!ok) {
-					atomicExch(err, 1);
-					stop = 1;
-				}
-			} else {
-				tile_apply<float, true>(sm, p.k, op, mats, base, highoff, p.L);
+			const TileOp& op = sops[oi];
+			const bool ok = op.nins == 5 ? tc_block<5>(sm, op, sB + op.lbit1, tmem, &mbar_mma, mma_phase)
+			                             : tc_block<4>(sm, op, sB + op.lbit1, tmem, &mbar_mma, mma_phase);
+			if (!ok) {
+				atomicExch(err, 1);
+				stop = 1;
 			}
 			__syncthreads();
 			if (stop) break;
 		}
 		if (stop) break;
 		{
-			float2 r[kBatch];
+			float2 r[kTcLoads];
 #pragma unroll
-			for (int b = 0; b < kBatch; ++b) r[b] = sm[threadIdx.x + b * kTileThreads];
+			for (int i = 0; i < kTcLoads; ++i) r[i] = sm[tid_off ^ tc_offset(kTcThreads * i)];
 #pragma unroll
-			for (int b = 0; b < kBatch; ++b) {
-				const uint32_t j = threadIdx.x + b * kTileThreads;
-				s[base | highoff[j >> p.L] | (j & lowmask)] = r[b];
+			for (int i = 0; i < kTcLoads; ++i) {
+				const uint32_t x = threadIdx.x + kTcThreads * i;
+				s[base | highoff[x >> p.L] | (x & lowmask)] = r[i];
 			}
 		}
 		__syncthreads();
@@ -739,8 +688,8 @@ cudaError_t launch_tile_pass(cplx_t<T>* s, const TilePass& p, const TileOp* d_op
 			    smem > kTcSmemLimit)
 				return cudaErrorInvalidValue;
 			const uint64_t ntiles = 1ULL << p.nfixed;
-			const uint64_t grid = std::min<uint64_t>(static_cast<uint64_t>(sms), ntiles);
-			k_tile_tc<<<static_cast<unsigned>(grid), kTileThreads, smem, st>>>(s, p, d_ops, d_mats, ntiles, d_err);
+			const uint64_t grid = std::min<uint64_t>(2ULL * static_cast<uint64_t>(sms), ntiles);
+			k_tile_tc<<<static_cast<unsigned>(grid), kTcThreads, smem, st>>>(s, p, d_ops, d_mats, ntiles, d_err);
 			note_launches(1);
 			return cudaGetLastError();
 		}
