@@ -62,11 +62,13 @@ def parse():
     ap.add_argument("--model", default=None, help="learned config: cost-model file")
     ap.add_argument("--config", default="layered", choices=["layered", "precision", "qaoa", "learned", "schrodinger"],
                     help="layered: the 30-qubit FP64 circuit (headline); precision: fused FP32 vs plain FP64")
-    ap.add_argument("--max-block", type=int, default=3, help="precision config: largest fused block")
+    ap.add_argument("--max-block", type=int, default=None, help="precision config: largest fused block (default: 3 and 5)")
     ap.add_argument("--no-fused", action="store_true", help="skip the fused-FP32 comparison in the layered line")
     ap.add_argument("--quick", action="store_true",
                     help="leave the precision (33 qubits), QAOA-batch and learned-fusion configurations out of the line")
-    return ap.parse_args()
+    args = ap.parse_args()
+    args.max_block_given = args.max_block is not None
+    return args
 
 
 def peaks():
@@ -504,8 +506,9 @@ def run_gb300(args):
     if rank == 0 and not args.no_fused:
         fops = [op for lay in layers[:4] for op in lay]
         extra["fused_fp32"] = {"workload": f"layers 0-3 of the circuit above ({len(fops)} gates); greedy blocks of at most "
-                                           "3 qubits, and the partition of the shipped learned cost model",
-                               **fused_vs_fp64(n, fops, 3, args.seed, learned=True)}
+                                           "5 qubits (4- and 5-qubit blocks on the tensor cores, the engine's default at this "
+                                           "size), and the partition of the shipped learned cost model",
+                               **fused_vs_fp64(n, fops, 5, args.seed, learned=True)}
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -516,7 +519,7 @@ def run_gb300(args):
         extra["c0"] = small_config_both(args.seed)
     if rank == 0 and world == 1 and not args.quick:
         reg.close()
-        extra["c2_precision"] = precision_config(33, 80, args.seed, 3)
+        extra["c2_precision"] = precision_config(33, 80, args.seed, (3, 5))
         extra["c3_qaoa"] = qaoa_config(args.seed, args.steps, dist=None)
         extra["c4_learned"] = learned_config(32, 100, args.seed, None)
 
@@ -654,22 +657,62 @@ def fused_vs_fp64(n: int, ops: list, max_block: int, seed: int = 1, learned: boo
     return res
 
 
-def precision_config(n: int, depth: int, seed: int, max_block: int) -> dict:
+def precision_config(n: int, depth: int, seed: int, blocks=(3, 5)) -> dict:
     """the precision configuration: the layered circuit on a plain FP64 register (16 * 2^n bytes) and on a
-    fused FP32 register (greedy blocks of at most max_block qubits, FP64 reductions): device time of
-    each, the speed-up, and the FP32 result's fidelity and max amplitude error against the FP64 one"""
-    from qcsim_gb300 import circuits
+    fused FP32 register (8 * 2^n bytes) with greedy blocks of at most 3 qubits (CUDA cores) and of at most
+    5 qubits (4- and 5-qubit blocks as 3xTF32 products on the tensor cores): device time of each, the
+    speed-up of the faster FP32 run, and every FP32 result's fidelity and max amplitude error against the
+    FP64 one"""
+    import ctypes as C
+    import torch
+    import qcsim_gb300 as Q
+    from qcsim_gb300 import _lib as L, circuits, gates as G
+    lib = L.load()
     ops = circuits.layered_circuit(n, depth, seed=seed)
-    res = fused_vs_fp64(n, ops, max_block, seed)
-    return {"workload": f"layered random circuit, {n} qubits, depth {depth}, seed {seed}; FP64 {16 << n >> 30} GiB, "
-                        f"FP32 {8 << n >> 30} GiB", **res}
+    recs = G.records(ops)
+    stream = torch.cuda.Stream()
+
+    def timed(reg):
+        lib.qcs_set_stream(reg.handle, stream.cuda_stream)
+        reg.profile(True)
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        reg.apply_records(recs)
+        b.record(stream)
+        b.synchronize()
+        prof = reg.read_profile()
+        reg.profile(False)
+        return a.elapsed_time(b) / 1e3, {k: {"launches": v[0], "ms": v[1]} for k, v in prof.items()}
+
+    r64 = Q.QubitRegister(n, seed=seed)
+    t64, k64 = timed(r64)
+    out = {"workload": f"layered random circuit, {n} qubits, depth {depth}, seed {seed}; FP64 {16 << n >> 30} GiB, "
+                       f"FP32 {8 << n >> 30} GiB", "gates": len(ops), "fp64_seconds": t64, "fp64_kernels": k64, "fp32_fused": {}}
+    for mb in blocks:
+        r32 = Q.QubitRegister(n, seed=seed, precision="fp32")
+        r32.set_fusion(1, mb)
+        t32, k32 = timed(r32)
+        f, d = C.c_double(), C.c_double()
+        L.check(lib.qcs_compare(r64.handle, r32.handle, C.byref(f), C.byref(d)), r64.handle)
+        out["fp32_fused"][f"max_block_{mb}"] = {"seconds": t32, "speedup": t64 / t32, "one_minus_fidelity": 1.0 - f.value,
+                                                 "max_abs_amplitude_error": d.value, "kernels": k32}
+        r32.close()
+    r64.close()
+    best = min(out["fp32_fused"], key=lambda k: out["fp32_fused"][k]["seconds"])
+    out.update({"best": best, "fp32_fused_seconds": out["fp32_fused"][best]["seconds"], "speedup": t64 / out["fp32_fused"][best]["seconds"],
+                "one_minus_fidelity": out["fp32_fused"][best]["one_minus_fidelity"],
+                "max_abs_amplitude_error": out["fp32_fused"][best]["max_abs_amplitude_error"]})
+    return out
 
 
 def run_precision(args):
-    """fused FP32 (dense blocks of <= max_block qubits) against plain FP64 on the same layered circuit"""
-    res = precision_config(args.qubits, args.depth, args.seed, args.max_block)
+    """fused FP32 (greedy blocks of at most --max-block qubits, and of at most 3 and 5 unless given)
+    against plain FP64 on the same layered circuit"""
+    blocks = (args.max_block,) if args.max_block_given else (3, 5)
+    res = precision_config(args.qubits, args.depth, args.seed, blocks)
     line = {"metric": "fused FP32 vs plain FP64 time @1-F<=1e-6", "config": {
-                "workload": res.pop("workload"), "gates": res.pop("gates"), "max_block_qubits": res.pop("max_block_qubits")},
+                "workload": res.pop("workload"), "gates": res.pop("gates"), "max_block_qubits": list(blocks)},
             **res, "data": "synthetic"}
     print(json.dumps(line))
 

@@ -293,7 +293,7 @@ double pass_fp_ops(const TilePass& tp, const std::vector<TileOp>& ops, int n) {
 }
 
 template <typename T>
-int run_planned(qcs_handle h, const std::vector<PlannedPass>& passes, int kmax, int L0) {
+int run_planned(qcs_handle h, const std::vector<PlannedPass>& passes, int kmax, int L0, bool tensor_passes = false) {
 	const int n = static_cast<int>(h->n);
 	std::vector<TilePass> tps;
 	std::vector<TileOp> ops;
@@ -342,9 +342,11 @@ int run_planned(qcs_handle h, const std::vector<PlannedPass>& passes, int kmax, 
 		tp.nfixed = nf;
 		tp.op_begin = static_cast<uint32_t>(ops.size());
 		uint32_t tc_slot = 0;  // bytes of resident block matrices used in this pass
-		// a tensor-core pass: FP32, a 12-qubit tile, and nothing but fused blocks (smaller ones are padded
-		// to 4 qubits); every operation of it runs on the tensor cores
-		bool tc_pass = sizeof(T) == 4 && h->tensor_cores && tp.k == kTcTileQubits && L >= 5 && tp.k - L <= 8 && !pp.gates.empty();
+		// a tensor-core pass: FP32, a fused gate list with a block of 4 or 5 qubits (apply_blocks), a 12-qubit
+		// tile, and nothing but fused blocks (smaller ones are widened to 4 qubits); every operation of it
+		// runs on the tensor cores
+		bool tc_pass = tensor_passes && sizeof(T) == 4 && h->tensor_cores && tp.k == kTcTileQubits && L >= 5 && tp.k - L <= 8 &&
+		               !pp.gates.empty();
 		for (const CompiledGate& c : pp.gates) tc_pass = tc_pass && c.kind == GKind::Block && !c.block_q.empty();
 		for (const CompiledGate& c : pp.gates) {
 			TileOp op;
@@ -600,7 +602,7 @@ int apply_blocks(qcs_handle h, std::vector<FusedBlock> blocks) {
 		passes.back().tmask = (1ULL << L0) - 1;
 	}
 	h->last_blocks = blocks.size();
-	return h->prec == QCS_FP64 ? run_planned<double>(h, passes, kmax, L0) : run_planned<float>(h, passes, kmax, L0);
+	return h->prec == QCS_FP64 ? run_planned<double>(h, passes, kmax, L0) : run_planned<float>(h, passes, kmax, L0, tc);
 }
 
 // the fused path: blocks of up to fusion_max qubits (or the partition the cost model picks)
@@ -618,7 +620,7 @@ int fused_apply(qcs_handle h, const qcs_gate* gates, size_t count) {
 		if (st != QCS_OK) return st;
 	} else {
 		FusionPolicy pol;
-		pol.max_qubits = std::min(h->fusion_max, h->prec == QCS_FP64 ? 4 : 5);
+		pol.max_qubits = std::min(h->fusion_limit(), h->prec == QCS_FP64 ? 4 : 5);
 		pol.nqubits = n;
 		blocks = fuse(cg, pol);
 	}

@@ -52,7 +52,7 @@ int choose_partition(qcs_handle h, const std::vector<CompiledGate>& gates, int k
                      double* predicted_ms) {
 	auto* cm = static_cast<CostModel*>(h->cost_ctx);
 	const int n = static_cast<int>(h->n);
-	const int top = std::min(h->fusion_max, h->prec == QCS_FP64 ? 4 : 5);
+	const int top = std::min(h->fusion_limit(), h->prec == QCS_FP64 ? 4 : 5);
 	double best_cost = 1e300;
 	for (int mq = 1; mq <= top; ++mq) {
 		FusionPolicy pol;

@@ -93,7 +93,7 @@ struct qcs_register {
 	void* batch = nullptr;                 // planner buffers (batch.cu)
 	int batch_mode = 1;                    // QCS_OPT_PASSES
 	int fusion = -1;                       // QCS_OPT_FUSION (-1: by precision)
-	int fusion_max = 3;                    // QCS_OPT_FUSION_MAX_QUBITS
+	int fusion_max = 0;                    // QCS_OPT_FUSION_MAX_QUBITS (0: by precision and size, fusion_limit)
 	int tensor_cores = 1;                  // QCS_OPT_TENSOR_CORES
 	void* cost_ctx = nullptr;              // learned partition choice (costmodel.cu)
 	double last_predicted_ms = 0;          // its prediction for the last fused gate list
@@ -105,6 +105,12 @@ struct qcs_register {
 	// stored values (amplitude / scale) stay far inside the precision's range
 	double scale_limit() const { return prec == QCS_FP64 ? 1e100 : 1e15; }
 	size_t state_bytes() const { return static_cast<size_t>(N) * amp_bytes(); }
+	// the largest fused block: the option when set; otherwise 5 for FP32 registers of at least 28 qubits
+	// with the tensor cores on (their tensor-core passes beat smaller blocks on the CUDA cores), else 3
+	int fusion_limit() const {
+		if (fusion_max > 0) return fusion_max;
+		return prec == QCS_FP32 && tensor_cores && n >= 28 ? 5 : 3;
+	}
 };
 
 namespace qcs {

@@ -558,7 +558,8 @@ __global__ void __launch_bounds__(kTcThreads, 2) k_tile_tc(float2* __restrict__ 
 	for (uint32_t i = threadIdx.x; i < p.op_count; i += blockDim.x) sops[i] = ops[p.op_begin + i];
 	build_fix_tables(fixtab, p);
 	const uint32_t warp = threadIdx.x >> 5;
-	const uint32_t lowmask = (1u << p.L) - 1;
+	const uint32_t L = static_cast<uint32_t>(p.L), nops = p.op_count;
+	const uint32_t lowmask = (1u << L) - 1;
 	const int nh = p.k - p.L;
 	for (uint32_t hh = threadIdx.x; hh < (1u << nh); hh += blockDim.x) {
 		uint64_t off = 0;
@@ -593,7 +594,7 @@ __global__ void __launch_bounds__(kTcThreads, 2) k_tile_tc(float2* __restrict__ 
 #pragma unroll
 		for (int i = 0; i < kTcLoads; ++i) {
 			const uint32_t x = threadIdx.x + kTcThreads * i;
-			pre[i] = s[b0 | highoff[x >> p.L] | (x & lowmask)];
+			pre[i] = s[b0 | highoff[x >> L] | (x & lowmask)];
 		}
 	}
 	for (uint64_t tile = blockIdx.x; tile < ntiles && !stop; tile += gridDim.x) {
@@ -606,11 +607,11 @@ __global__ void __launch_bounds__(kTcThreads, 2) k_tile_tc(float2* __restrict__ 
 #pragma unroll
 			for (int i = 0; i < kTcLoads; ++i) {
 				const uint32_t x = threadIdx.x + kTcThreads * i;
-				pre[i] = s[nb | highoff[x >> p.L] | (x & lowmask)];
+				pre[i] = s[nb | highoff[x >> L] | (x & lowmask)];
 			}
 		}
 		__syncthreads();
-		for (uint32_t oi = 0; oi < p.op_count; ++oi) {
+		for (uint32_t oi = 0; oi < nops; ++oi) {
 			const TileOp& op = sops[oi];
 			const bool ok = op.nins == 5 ? tc_block<5>(sm, op, sB + op.lbit1, tmem, &mbar_mma, mma_phase)
 			                             : tc_block<4>(sm, op, sB + op.lbit1, tmem, &mbar_mma, mma_phase);
@@ -629,7 +630,7 @@ __global__ void __launch_bounds__(kTcThreads, 2) k_tile_tc(float2* __restrict__ 
 #pragma unroll
 			for (int i = 0; i < kTcLoads; ++i) {
 				const uint32_t x = threadIdx.x + kTcThreads * i;
-				s[base | highoff[x >> p.L] | (x & lowmask)] = r[i];
+				s[base | highoff[x >> L] | (x & lowmask)] = r[i];
 			}
 		}
 		__syncthreads();
