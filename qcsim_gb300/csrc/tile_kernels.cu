@@ -455,6 +455,13 @@ __host__ __device__ constexpr uint32_t tc_offset(uint32_t x) {
 	return o;
 }
 
+// per block of a pass, computed once per CTA: the swizzled offset of every row index inside an M tile, and
+// w[0..4] = the offsets of the block bits, w[5] = that of the M-tile row bit (K = 4)
+struct TcTab {
+	uint16_t row[128];
+	uint16_t w[8];
+};
+
 // one block of K = 4 or 5 qubits on the tile: gather and split into tensor memory, 3xTF32 MMAs, then the
 // outputs back into the tile.  false when the MMA completion wait ran out.
 //   K = 5: one M tile (128 columns of 32 amplitudes); warp w: lanes 32 (w % 4) + 0..31, amplitudes
@@ -462,7 +469,8 @@ __host__ __device__ constexpr uint32_t tc_offset(uint32_t x) {
 //   K = 4: two M tiles (256 columns of 16 amplitudes); warp w: M tile w / 4, lanes 32 (w % 4) + 0..31,
 //          all 16 amplitudes
 template <int K>
-__device__ bool tc_block(float2* sm, const TileOp& op, const unsigned char* sBop, uint32_t tmem, uint64_t* mbar, uint32_t& phase) {
+__device__ bool tc_block(float2* sm, const TcTab& tab, const unsigned char* sBop, uint32_t tmem, uint64_t* mbar, uint32_t& phase,
+                         int* mma_ok) {
 	constexpr uint32_t D = 1u << K, kdim = 2 * D;
 	constexpr uint32_t sbo_b = (kdim / 4) * 128;
 	const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
@@ -471,13 +479,10 @@ __device__ bool tc_block(float2* sm, const TileOp& op, const unsigned char* sBop
 	// swizzled offsets of the block bits and of this thread's row
 	uint32_t bw[K];
 #pragma unroll
-	for (int t = 0; t < K; ++t) bw[t] = tc_bit_offset(static_cast<int>((op.ins >> (8 * t)) & 0xffu));
-	uint32_t rb = 0;
-#pragma unroll
-	for (int r = 0; r < 7; ++r)
-		if ((m >> r) & 1u) rb ^= tc_bit_offset(static_cast<int>((op.gtbit >> (4 * r)) & 15u));
-	if (K == 4 && h) rb ^= tc_bit_offset(static_cast<int>((op.gtbit >> 28) & 15u));  // the M tile's row bit
-	if (K == 5 && h) rb ^= bw[K - 1];                                                  // j = 16 h + jj
+	for (int t = 0; t < K; ++t) bw[t] = tab.w[t];
+	uint32_t rb = tab.row[m];
+	if (K == 4 && h) rb ^= tab.w[5];     // the M tile's row bit
+	if (K == 5 && h) rb ^= bw[K - 1];    // j = 16 h + jj
 	// tensor-memory columns of this thread's A values and accumulators
 	const uint32_t lanes = (32u * quad) << 16;
 	const uint32_t a_hi = K == 5 ? kTcAcol + 32u * h : kTcAcol + 64u * h;
@@ -495,8 +500,8 @@ __device__ bool tc_block(float2* sm, const TileOp& op, const unsigned char* sBop
 			const float hx = tf32_rna(v.x), hy = tf32_rna(v.y);
 			hi[2 * u] = hx;
 			hi[2 * u + 1] = hy;
-			lo[2 * u] = tf32_rna(v.x - hx);
-			lo[2 * u + 1] = tf32_rna(v.y - hy);
+			lo[2 * u] = v.x - hx;  // exact; the tensor core reads it as TF32
+			lo[2 * u + 1] = v.y - hy;
 		}
 		tc::tmem_st16(tmem + lanes + a_hi + 16u * c8, hi);
 		tc::tmem_st16(tmem + lanes + a_lo + 16u * c8, lo);
@@ -523,10 +528,15 @@ __device__ bool tc_block(float2* sm, const TileOp& op, const unsigned char* sBop
 			}
 		}
 		tc::mma_commit(mbar);
+		// the issuing thread alone waits for the MMAs (bounded); the others wait at the barrier below
+		// instead of polling the mbarrier, which leaves the issue slots to the SM's other CTA
+		*mma_ok = tc::mbar_wait(mbar, phase, kTcWaitTries) ? 1 : 0;
+		tc::fence_before_sync();
 	}
-	const bool ok = tc::mbar_wait(mbar, phase, kTcWaitTries);
-	phase ^= 1u;
+	__syncthreads();
 	tc::fence_after_sync();
+	const bool ok = *mma_ok != 0;
+	phase ^= 1u;
 #pragma unroll
 	for (uint32_t c8 = 0; c8 < 2; ++c8) {
 		float v[16], w[16];
@@ -551,11 +561,27 @@ __global__ void __launch_bounds__(kTcThreads, 2) k_tile_tc(float2* __restrict__ 
 	__shared__ __align__(8) uint64_t mbar_mma;
 	__shared__ uint32_t tmem_slot;
 	__shared__ int stop;
+	__shared__ int mma_ok;
 	float2* sm = reinterpret_cast<float2*>(smraw);
 	unsigned char* sB = smraw + kTcTileBytes;
-	// the pass's operations, copied once (behind the block matrices)
+	// the pass's operations, copied once (behind the block matrices), and their row tables
 	TileOp* sops = reinterpret_cast<TileOp*>(sB + kTcMatBudget);
-	for (uint32_t i = threadIdx.x; i < p.op_count; i += blockDim.x) sops[i] = ops[p.op_begin + i];
+	TcTab* tabs = reinterpret_cast<TcTab*>(sops + p.op_count);
+	for (uint32_t i = threadIdx.x; i < p.op_count; i += blockDim.x) {
+		const TileOp op = ops[p.op_begin + i];
+		sops[i] = op;
+		for (int t = 0; t < 8; ++t)
+			tabs[i].w[t] = static_cast<uint16_t>(t < op.nins ? tc_bit_offset(static_cast<int>((op.ins >> (8 * t)) & 0xffu))
+			                                     : (t == 5 ? tc_bit_offset(static_cast<int>((op.gtbit >> 28) & 15u)) : 0u));
+	}
+	for (uint32_t e = threadIdx.x; e < p.op_count * 128u; e += blockDim.x) {
+		const uint32_t i = e >> 7, m = e & 127u;
+		const uint64_t order = ops[p.op_begin + i].gtbit;
+		uint32_t o = 0;
+		for (int r = 0; r < 7; ++r)
+			if ((m >> r) & 1u) o ^= tc_bit_offset(static_cast<int>((order >> (4 * r)) & 15u));
+		tabs[i].row[m] = static_cast<uint16_t>(o);
+	}
 	build_fix_tables(fixtab, p);
 	const uint32_t warp = threadIdx.x >> 5;
 	const uint32_t L = static_cast<uint32_t>(p.L), nops = p.op_count;
@@ -613,8 +639,8 @@ __global__ void __launch_bounds__(kTcThreads, 2) k_tile_tc(float2* __restrict__ 
 		__syncthreads();
 		for (uint32_t oi = 0; oi < nops; ++oi) {
 			const TileOp& op = sops[oi];
-			const bool ok = op.nins == 5 ? tc_block<5>(sm, op, sB + op.lbit1, tmem, &mbar_mma, mma_phase)
-			                             : tc_block<4>(sm, op, sB + op.lbit1, tmem, &mbar_mma, mma_phase);
+			const bool ok = op.nins == 5 ? tc_block<5>(sm, tabs[oi], sB + op.lbit1, tmem, &mbar_mma, mma_phase, &mma_ok)
+			                             : tc_block<4>(sm, tabs[oi], sB + op.lbit1, tmem, &mbar_mma, mma_phase, &mma_ok);
 			if (!ok) {
 				atomicExch(err, 1);
 				stop = 1;
@@ -684,7 +710,7 @@ cudaError_t launch_tile_pass(cplx_t<T>* s, const TilePass& p, const TileOp* d_op
 					tc_configured[dev] = true;
 				}
 			}
-			const size_t smem = kTcSmem + static_cast<size_t>(p.op_count) * sizeof(TileOp);
+			const size_t smem = kTcSmem + static_cast<size_t>(p.op_count) * (sizeof(TileOp) + sizeof(TcTab));
 			if (p.k != kTcTileQubits || p.L < 5 || p.k - p.L > kMaxHigh || p.nfixed > 8 * kFixChunks || !d_err ||
 			    smem > kTcSmemLimit)
 				return cudaErrorInvalidValue;
