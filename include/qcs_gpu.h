@@ -232,7 +232,7 @@ int qcs_fusion_plan(uint32_t nqubits, const qcs_gate* gates, size_t count, int m
 int qcs_fusion_passes(uint32_t nqubits, const qcs_gate* gates, size_t count, int max_qubits, int tile_qubits, int tensor_cores,
                       uint32_t* pass_of_block, size_t capacity, size_t* nblocks_out, size_t* npasses_out);
 /* attach a trained model (kept by the caller) and the measured time of one pass per register size
- * (pass_ms[n], milliseconds); NULL detaches */
+ * (pass_ms[n], milliseconds; with len >= 128, pass_ms[64 + n] is that of a tensor-core pass); NULL detaches */
 int qcs_set_cost_model(qcs_handle h, qcs_mlp_handle mlp, const double* pass_ms, size_t len);
 
 /* ---- engine options ---- */
@@ -241,9 +241,9 @@ enum qcs_option {
 	QCS_OPT_FUSION = 2,          /* gate lists fused into dense blocks: 0 off (FP64 default), 1 greedy (FP32
 	                                default), 2 partition chosen by the learned cost model when one is loaded */
 	QCS_OPT_FUSION_MAX_QUBITS = 3, /* largest fused block (1..5; FP64 registers use at most 4).  Default: 5 on FP32
-	                                  registers of 28 or more qubits with the tensor cores on (4- and 5-qubit blocks
+	                                  registers of 26 or more qubits with the tensor cores on (4- and 5-qubit blocks
 	                                  on tcgen05 beat blocks of at most 3 on the CUDA cores there), else 3; the
-	                                  learned partition mixes sizes */
+	                                  learned partition chooses per gate list */
 	QCS_OPT_TENSOR_CORES = 4       /* FP32 registers: 1 (default) fused blocks of 4 and 5 qubits run as 3xTF32
 	                                  products on the tensor cores (tcgen05); 0: FP32 FMAs on the CUDA cores */
 };

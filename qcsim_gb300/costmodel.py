@@ -196,52 +196,56 @@ def _pass_ms(prof: dict) -> float:
     return sum(v[1] for k, v in prof.items() if k.startswith("tile_pass")) / launches
 
 
-def time_blocks(samples, reps: int = 3, seed: int = 0, log=print) -> tuple[np.ndarray, np.ndarray, dict]:
-    """device time of each sampled block applied alone in a pass, minus the time of a pass over the same
-    register with a one-qubit identity (the memory cost every pass pays): returns features, log(ms)
-    targets and the per-size pass times"""
+def time_blocks(samples, reps: int = 3, seed: int = 0, log=print) -> tuple[np.ndarray, np.ndarray, dict, dict]:
+    """device time of each sampled block applied alone in a pass, minus the time of the same kind of pass
+    over the same register that carries only an identity (the memory cost every pass pays): blocks of
+    4 and 5 qubits run in tensor-core passes (the identity there is a 4-qubit one), smaller blocks in
+    CUDA-core passes (a one-qubit identity).  Returns features, log(ms) targets and the per-size pass
+    times of both kinds."""
     import torch
     from .register import QubitRegister
     rng = np.random.default_rng(seed)
     by_n: dict[int, list] = {}
     for s in samples:
         by_n.setdefault(s[0], []).append(s)
-    X, T, pass_ms = [], [], {}
+    X, T, pass_ms, pass_ms_tc = [], [], {}, {}
+
+    def pass_time(reg, qubits, m) -> float:
+        apply_matrix(reg, qubits, m)  # warm
+        reg.read_profile()
+        for _ in range(reps):
+            apply_matrix(reg, qubits, m)
+        return _pass_ms(reg.read_profile())
+
     for n in sorted(by_n):
         reg = QubitRegister(n, seed=1, precision="fp32")
         reg.profile(True)
-        eye = np.eye(2, dtype=np.complex128)
-        for _ in range(2):
-            apply_matrix(reg, [0], eye)
-        reg.read_profile()
-        for _ in range(reps):
-            apply_matrix(reg, [0], eye)
-        p = reg.read_profile()
-        base = _pass_ms(p)
-        pass_ms[n] = base
+        base = pass_time(reg, [0], np.eye(2, dtype=np.complex128))
+        base_tc = pass_time(reg, [0, 1, 2, 3], np.eye(16, dtype=np.complex128))
+        pass_ms[n], pass_ms_tc[n] = base, base_tc
         for (nn, qubits, ng) in by_n[n]:
             u = random_unitary(len(qubits), rng)
-            apply_matrix(reg, list(qubits), u)  # warm
-            reg.read_profile()
-            for _ in range(reps):
-                apply_matrix(reg, list(qubits), u)
-            p = reg.read_profile()
-            ms = _pass_ms(p)
+            ms = pass_time(reg, list(qubits), u)
+            b = base_tc if len(qubits) >= 4 else base
             X.append(features(n, qubits, ng))
-            T.append(math.log(max(ms - base, 0.02 * base)))
+            T.append(math.log(max(ms - b, 0.02 * b)))
         reg.profile(False)
         reg.close()
         torch.cuda.synchronize()
-        log(f"n={n}: {len(by_n[n])} blocks timed, pass {base:.3f} ms")
-    return np.array(X, dtype=np.float32), np.array(T, dtype=np.float32), pass_ms
+        log(f"n={n}: {len(by_n[n])} blocks timed, pass {base:.3f} ms, tensor-core pass {base_tc:.3f} ms")
+    return np.array(X, dtype=np.float32), np.array(T, dtype=np.float32), pass_ms, pass_ms_tc
 
 
-def save(mlp: Mlp, pass_ms: dict, path: Path | None = None, meta: dict | None = None) -> Path:
+def save(mlp: Mlp, pass_ms: dict, path: Path | None = None, meta: dict | None = None, pass_ms_tc: dict | None = None) -> Path:
+    """the parameters and a 128-entry table: [n] = one CUDA-core pass over n qubits, [64 + n] = one
+    tensor-core pass (0 where not measured)"""
     path = path or (MODEL_DIR / "fusion_cost_mlp.npz")
     path.parent.mkdir(exist_ok=True)
-    table = np.zeros(64)
+    table = np.zeros(128)
     for n, v in pass_ms.items():
         table[int(n)] = v
+    for n, v in (pass_ms_tc or {}).items():
+        table[64 + int(n)] = v
     np.savez(path, params=mlp.params(), pass_ms=table, **{k: np.asarray(v) for k, v in (meta or {}).items()})
     return path
 
@@ -251,7 +255,9 @@ def load(path: Path | None = None) -> tuple[Mlp, np.ndarray]:
     d = np.load(path)
     m = Mlp(F)
     m.set_params(d["params"])
-    return m, d["pass_ms"]
+    table = np.zeros(128)
+    table[: d["pass_ms"].size] = d["pass_ms"]
+    return m, table
 
 
 def attach(reg, mlp: Mlp, pass_ms: np.ndarray) -> None:
@@ -307,14 +313,15 @@ def _main() -> None:
         chosen += by_w[w][:per]
     chosen = [(n, q, distinct[(n, q)]) for (n, q) in chosen]
     t1 = time.time()
-    X, T, pass_ms = time_blocks(chosen)
+    X, T, pass_ms, pass_ms_tc = time_blocks(chosen)
     t2 = time.time()
     mlp, metrics = train_from_timings(X, T)
     t3 = time.time()
     metrics.update({"circuits": args.circuits, "blocks_sampled": len(samples), "distinct_blocks": len(distinct),
                     "blocks_timed": len(chosen), "seconds_sampling": t1 - t0, "seconds_timing": t2 - t1,
-                    "seconds_training": t3 - t2, "pass_ms": {str(k): v for k, v in pass_ms.items()}})
-    path = save(mlp, pass_ms, Path(args.out), meta={"X": X, "T": T})
+                    "seconds_training": t3 - t2, "pass_ms": {str(k): v for k, v in pass_ms.items()},
+                    "pass_ms_tc": {str(k): v for k, v in pass_ms_tc.items()}})
+    path = save(mlp, pass_ms, Path(args.out), meta={"X": X, "T": T}, pass_ms_tc=pass_ms_tc)
     print(json.dumps({"model": str(path), **metrics}))
 
 

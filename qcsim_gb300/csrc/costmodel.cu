@@ -1,10 +1,12 @@
 // The learned partition choice of the FP32 path and the dense k-qubit operator entry point.
 //
 // A fused block's features (its width, gate count, qubit positions, register size) feed the MLP of
-// mlp.cu, which predicts the log of the block's marginal device time inside a shared-memory pass.  A
-// candidate partition (the greedy fuser run with a given largest block) is scored as
+// mlp.cu, which predicts the log of the block's marginal device time inside a shared-memory pass (a
+// tensor-core pass for blocks of 4 and 5 qubits, a CUDA-core pass for smaller ones).  A candidate
+// partition (the greedy fuser run with a given largest block) is scored as
 //   sum over blocks of exp(prediction) + passes x (time of one pass over the register),
-// and the cheapest candidate is applied.
+// with the tensor-core pass time when the candidate runs on the tensor cores (its smaller blocks then
+// scored as the 4-qubit blocks they are widened to), and the cheapest candidate is applied.
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -40,7 +42,7 @@ void block_features(int n, const uint32_t* q, uint32_t m, uint32_t ngates, float
 
 struct CostModel {
 	qcs_mlp_handle mlp = nullptr;
-	std::vector<double> pass_ms;  // index: register qubits
+	std::vector<double> pass_ms;  // index: register qubits; entries 64 + n (when given): a tensor-core pass
 };
 
 // passes the planner forms for these blocks (the packing of apply_blocks)
@@ -59,9 +61,19 @@ int choose_partition(qcs_handle h, const std::vector<CompiledGate>& gates, int k
 		pol.max_qubits = mq;
 		pol.nqubits = n;
 		std::vector<FusedBlock> cand = fuse(gates, pol);
+		bool big = false;
+		for (const FusedBlock& b : cand) big = big || b.qubits.size() >= 4;
+		const bool tc = h->prec == QCS_FP32 && h->tensor_cores && big && n >= kTcTileQubits;
 		std::vector<float> x(cand.size() * kFeatures);
-		for (size_t i = 0; i < cand.size(); ++i)
-			block_features(n, cand[i].qubits.data(), static_cast<uint32_t>(cand[i].qubits.size()), cand[i].ngates, &x[i * kFeatures]);
+		for (size_t i = 0; i < cand.size(); ++i) {
+			// in tensor-core passes a smaller block runs widened to 4 qubits (the lowest ones it lacks)
+			std::vector<uint32_t> q = cand[i].qubits;
+			if (tc && !q.empty())
+				for (uint32_t b = 0; q.size() < 4 && b < static_cast<uint32_t>(n); ++b)
+					if (std::find(q.begin(), q.end(), b) == q.end()) q.push_back(b);
+			std::sort(q.begin(), q.end());
+			block_features(n, q.data(), static_cast<uint32_t>(q.size()), cand[i].ngates, &x[i * kFeatures]);
+		}
 		std::vector<float> y(cand.size());
 		if (!cand.empty()) {
 			const int st = qcs_mlp_predict(cm->mlp, x.data(), static_cast<int>(cand.size()), y.data());
@@ -69,10 +81,10 @@ int choose_partition(qcs_handle h, const std::vector<CompiledGate>& gates, int k
 		}
 		double cost = 0;
 		for (float v : y) cost += std::exp(static_cast<double>(v));
-		const double pms = static_cast<size_t>(n) < cm->pass_ms.size() ? cm->pass_ms[static_cast<size_t>(n)] : 0.0;
-		bool big = false;
-		for (const FusedBlock& b : cand) big = big || b.qubits.size() >= 4;
-		const bool tc = h->prec == QCS_FP32 && h->tensor_cores && big;
+		const size_t ti = 64 + static_cast<size_t>(n);
+		const double pms = tc && ti < cm->pass_ms.size() && cm->pass_ms[ti] > 0
+		                       ? cm->pass_ms[ti]
+		                       : (static_cast<size_t>(n) < cm->pass_ms.size() ? cm->pass_ms[static_cast<size_t>(n)] : 0.0);
 		cost += pms * count_passes(cand, tc ? std::min(kmax, kTcTileQubits) : kmax, L0, tc);
 		if (cost < best_cost) {
 			best_cost = cost;
