@@ -14,13 +14,13 @@ applied over their CUDA-event time; DRAM traffic per launch from the committed n
 kernel's FP64-compute ceiling (`fp64_roofline`: FP64 instructions of its gate arithmetic per second
 against cuBLAS DGEMM measured in the same run), the same layers with one kernel per gate (`per_gate`),
 QFT-30 (`qft`), the first four layers on fused FP32 registers against FP64 (`fused_fp32`: greedy blocks
-of at most 3 qubits and the learned partition), the 20-qubit depth-40 circuit timed whole on the GPU and
+of at most 5 qubits on the tensor cores and the learned partition), the 20-qubit depth-40 circuit timed whole on the GPU and
 on the CPU reference (`c0`), SM clocks sampled during the timed region, and the CPU reference on a bounded
 sample (`cpu_baseline`: QCSim's own QubitRegister compiled on the host where its sources were staged,
 else the oracle's restatement; OpenMP on all host threads).  `parity_at_size` checks the engine against
 that CPU reference at the full size: the baseline's gate sample, the QFT of a random normal state, and
 1024 seeded shots from it.  Unless --quick, the line also carries the other configurations:
-`c2_precision` (33 qubits, depth 80: fused FP32 against plain FP64), `c3_qaoa` (512 QAOA instances, p = 4,
+`c2_precision` (33 qubits, depth 80: fused FP32 with blocks of at most 3 and 5 qubits against plain FP64), `c3_qaoa` (512 QAOA instances, p = 4,
 one launch, FP64 and FP32) and `c4_learned` (an unseen 32-qubit circuit of depth 100 with 10% controlled
 rotations: the learned partition against both greedy fusers and unfused FP64).
 
@@ -502,7 +502,7 @@ def run_gb300(args):
                         "hbm_frac_per_gate": qb / (qft_ms / 1e3) / (peak * 1e9)}
 
     # the metric's second half on the same circuit: its first four layers on a fresh FP64 register and on
-    # fused FP32 registers (greedy blocks of at most 3 qubits; the learned partition), device time and fidelity
+    # fused FP32 registers (greedy blocks of at most 5 qubits; the learned partition), device time and fidelity
     if rank == 0 and not args.no_fused:
         fops = [op for lay in layers[:4] for op in lay]
         extra["fused_fp32"] = {"workload": f"layers 0-3 of the circuit above ({len(fops)} gates); greedy blocks of at most "
