@@ -197,11 +197,12 @@ def _pass_ms(prof: dict) -> float:
 
 
 def time_blocks(samples, reps: int = 3, seed: int = 0, log=print) -> tuple[np.ndarray, np.ndarray, dict, dict]:
-    """device time of each sampled block applied alone in a pass, minus the time of the same kind of pass
-    over the same register that carries only an identity (the memory cost every pass pays): blocks of
-    4 and 5 qubits run in tensor-core passes (the identity there is a 4-qubit one), smaller blocks in
-    CUDA-core passes (a one-qubit identity).  Returns features, log(ms) targets and the per-size pass
-    times of both kinds."""
+    """device time of each sampled block applied alone in a pass, minus the time of a CUDA-core pass over
+    the same register that carries only a one-qubit identity (the memory cost every pass pays).  Blocks
+    of 4 and 5 qubits run in tensor-core passes, smaller ones in CUDA-core passes; a block's target is
+    thus its whole cost beyond streaming the register once.  Returns features, log(ms) targets and the
+    per-size times of the identity passes of both kinds (the tensor-core one carries a 4-qubit
+    identity block)."""
     import torch
     from .register import QubitRegister
     rng = np.random.default_rng(seed)
@@ -226,9 +227,8 @@ def time_blocks(samples, reps: int = 3, seed: int = 0, log=print) -> tuple[np.nd
         for (nn, qubits, ng) in by_n[n]:
             u = random_unitary(len(qubits), rng)
             ms = pass_time(reg, list(qubits), u)
-            b = base_tc if len(qubits) >= 4 else base
             X.append(features(n, qubits, ng))
-            T.append(math.log(max(ms - b, 0.02 * b)))
+            T.append(math.log(max(ms - base, 0.02 * base)))
         reg.profile(False)
         reg.close()
         torch.cuda.synchronize()

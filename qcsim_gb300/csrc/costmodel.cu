@@ -4,9 +4,9 @@
 // mlp.cu, which predicts the log of the block's marginal device time inside a shared-memory pass (a
 // tensor-core pass for blocks of 4 and 5 qubits, a CUDA-core pass for smaller ones).  A candidate
 // partition (the greedy fuser run with a given largest block) is scored as
-//   sum over blocks of exp(prediction) + passes x (time of one pass over the register),
-// with the tensor-core pass time when the candidate runs on the tensor cores (its smaller blocks then
-// scored as the 4-qubit blocks they are widened to), and the cheapest candidate is applied.
+//   sum over blocks of exp(prediction) + passes x (time of one streaming pass over the register),
+// a candidate on the tensor cores scoring its smaller blocks as the 4-qubit blocks they are widened to,
+// and the cheapest candidate is applied.
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -42,7 +42,7 @@ void block_features(int n, const uint32_t* q, uint32_t m, uint32_t ngates, float
 
 struct CostModel {
 	qcs_mlp_handle mlp = nullptr;
-	std::vector<double> pass_ms;  // index: register qubits; entries 64 + n (when given): a tensor-core pass
+	std::vector<double> pass_ms;  // index: register qubits (entries 64 + n, when given: a tensor-core pass, not used)
 };
 
 // passes the planner forms for these blocks (the packing of apply_blocks)
@@ -81,10 +81,9 @@ int choose_partition(qcs_handle h, const std::vector<CompiledGate>& gates, int k
 		}
 		double cost = 0;
 		for (float v : y) cost += std::exp(static_cast<double>(v));
-		const size_t ti = 64 + static_cast<size_t>(n);
-		const double pms = tc && ti < cm->pass_ms.size() && cm->pass_ms[ti] > 0
-		                       ? cm->pass_ms[ti]
-		                       : (static_cast<size_t>(n) < cm->pass_ms.size() ? cm->pass_ms[static_cast<size_t>(n)] : 0.0);
+		// every block's predicted cost is its whole cost beyond one streaming pass over the register, so the
+		// pass term is the CUDA-core pass time for both kinds of candidate
+		const double pms = static_cast<size_t>(n) < cm->pass_ms.size() ? cm->pass_ms[static_cast<size_t>(n)] : 0.0;
 		cost += pms * count_passes(cand, tc ? std::min(kmax, kTcTileQubits) : kmax, L0, tc);
 		if (cost < best_cost) {
 			best_cost = cost;
