@@ -14,15 +14,16 @@ applied over their CUDA-event time; DRAM traffic per launch from the committed n
 kernel's FP64-compute ceiling (`fp64_roofline`: FP64 instructions of its gate arithmetic per second
 against cuBLAS DGEMM measured in the same run), the same layers with one kernel per gate (`per_gate`),
 QFT-30 (`qft`), the first four layers on fused FP32 registers against FP64 (`fused_fp32`: greedy blocks
-of at most 5 qubits on the tensor cores and the learned partition), the 20-qubit depth-40 circuit timed whole on the GPU and
+of at most 4 qubits on the tensor cores and the learned partition), the 20-qubit depth-40 circuit timed whole on the GPU and
 on the CPU reference (`c0`), SM clocks sampled during the timed region, and the CPU reference on a bounded
 sample (`cpu_baseline`: QCSim's own QubitRegister compiled on the host where its sources were staged,
 else the oracle's restatement; OpenMP on all host threads).  `parity_at_size` checks the engine against
 that CPU reference at the full size: the baseline's gate sample, the QFT of a random normal state, and
 1024 seeded shots from it.  Unless --quick, the line also carries the other configurations:
-`c2_precision` (33 qubits, depth 80: fused FP32 with blocks of at most 3 and 5 qubits against plain FP64), `c3_qaoa` (512 QAOA instances, p = 4,
+`c2_precision` (33 qubits, depth 80: fused FP32 with blocks of at most 3, 4 and 5 qubits against plain FP64), `c3_qaoa` (512 QAOA instances, p = 4,
 one launch, FP64 and FP32) and `c4_learned` (an unseen 32-qubit circuit of depth 100 with 10% controlled
-rotations: the learned partition against both greedy fusers and unfused FP64).
+rotations: the learned partition against the greedy fuser with largest blocks of 3, 4 and 5 qubits and
+unfused FP64).
 
 --impl reference times the same CPU reference on the same workload, a bounded number of gates per step.
 The configurations also run alone: --config precision, qaoa (sharded over ranks under torchrun), learned,
@@ -62,7 +63,7 @@ def parse():
     ap.add_argument("--model", default=None, help="learned config: cost-model file")
     ap.add_argument("--config", default="layered", choices=["layered", "precision", "qaoa", "learned", "schrodinger"],
                     help="layered: the 30-qubit FP64 circuit (headline); precision: fused FP32 vs plain FP64")
-    ap.add_argument("--max-block", type=int, default=None, help="precision config: largest fused block (default: 3 and 5)")
+    ap.add_argument("--max-block", type=int, default=None, help="precision config: largest fused block (default: 3, 4 and 5)")
     ap.add_argument("--no-fused", action="store_true", help="skip the fused-FP32 comparison in the layered line")
     ap.add_argument("--quick", action="store_true",
                     help="leave the precision (33 qubits), QAOA-batch and learned-fusion configurations out of the line")
@@ -502,13 +503,13 @@ def run_gb300(args):
                         "hbm_frac_per_gate": qb / (qft_ms / 1e3) / (peak * 1e9)}
 
     # the metric's second half on the same circuit: its first four layers on a fresh FP64 register and on
-    # fused FP32 registers (greedy blocks of at most 5 qubits; the learned partition), device time and fidelity
+    # fused FP32 registers (greedy blocks of at most 4 qubits; the learned partition), device time and fidelity
     if rank == 0 and not args.no_fused:
         fops = [op for lay in layers[:4] for op in lay]
         extra["fused_fp32"] = {"workload": f"layers 0-3 of the circuit above ({len(fops)} gates); greedy blocks of at most "
-                                           "5 qubits (4- and 5-qubit blocks on the tensor cores, the engine's default at this "
-                                           "size), and the partition of the shipped learned cost model",
-                               **fused_vs_fp64(n, fops, 5, args.seed, learned=True)}
+                                           "4 qubits on the tensor cores (the engine's default at this size), and the partition "
+                                           "of the shipped learned cost model",
+                               **fused_vs_fp64(n, fops, 4, args.seed, learned=True)}
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -519,7 +520,7 @@ def run_gb300(args):
         extra["c0"] = small_config_both(args.seed)
     if rank == 0 and world == 1 and not args.quick:
         reg.close()
-        extra["c2_precision"] = precision_config(33, 80, args.seed, (3, 5))
+        extra["c2_precision"] = precision_config(33, 80, args.seed, (3, 4, 5))
         extra["c3_qaoa"] = qaoa_config(args.seed, args.steps, dist=None)
         extra["c4_learned"] = learned_config(32, 100, args.seed, None)
 
@@ -657,10 +658,10 @@ def fused_vs_fp64(n: int, ops: list, max_block: int, seed: int = 1, learned: boo
     return res
 
 
-def precision_config(n: int, depth: int, seed: int, blocks=(3, 5)) -> dict:
+def precision_config(n: int, depth: int, seed: int, blocks=(3, 4, 5)) -> dict:
     """the precision configuration: the layered circuit on a plain FP64 register (16 * 2^n bytes) and on a
     fused FP32 register (8 * 2^n bytes) with greedy blocks of at most 3 qubits (CUDA cores) and of at most
-    5 qubits (4- and 5-qubit blocks as 3xTF32 products on the tensor cores): device time of each, the
+    4 and 5 qubits (every block as a 3xTF32 product on the tensor cores): device time of each, the
     speed-up of the faster FP32 run, and every FP32 result's fidelity and max amplitude error against the
     FP64 one"""
     import ctypes as C
@@ -709,7 +710,7 @@ def precision_config(n: int, depth: int, seed: int, blocks=(3, 5)) -> dict:
 def run_precision(args):
     """fused FP32 (greedy blocks of at most --max-block qubits, and of at most 3 and 5 unless given)
     against plain FP64 on the same layered circuit"""
-    blocks = (args.max_block,) if args.max_block_given else (3, 5)
+    blocks = (args.max_block,) if args.max_block_given else (3, 4, 5)
     res = precision_config(args.qubits, args.depth, args.seed, blocks)
     line = {"metric": "fused FP32 vs plain FP64 time @1-F<=1e-6", "config": {
                 "workload": res.pop("workload"), "gates": res.pop("gates"), "max_block_qubits": list(blocks)},
@@ -790,7 +791,7 @@ def run_qaoa(args):
 def learned_config(n: int, depth: int, seed: int, model: str | None) -> dict:
     """learned fusion on an unseen circuit (n qubits, depth, 10% of one-qubit slots controlled
     rotations): device time and fidelity of the FP32 path with the MLP's partition, with the greedy
-    fuser (largest block 3 and 5), and of the unfused plain FP64 path.  Each FP32 time includes the
+    fuser (largest block 3, 4 and 5), and of the unfused plain FP64 path.  Each FP32 time includes the
     partition search and planning of its first (and only) call."""
     import ctypes as C
     import torch
@@ -815,8 +816,8 @@ def learned_config(n: int, depth: int, seed: int, model: str | None) -> dict:
     r64 = Q.QubitRegister(n, seed=1)
     t64 = timed(r64)
     res = {"fp64_unfused_seconds": t64}
-    for name, setup in (("greedy5", lambda r: r.set_fusion(1, 5)), ("greedy3", lambda r: r.set_fusion(1, 3)),
-                        ("learned", lambda r: costmodel.attach(r, mlp, pass_ms))):
+    for name, setup in (("greedy5", lambda r: r.set_fusion(1, 5)), ("greedy4", lambda r: r.set_fusion(1, 4)),
+                        ("greedy3", lambda r: r.set_fusion(1, 3)), ("learned", lambda r: costmodel.attach(r, mlp, pass_ms))):
         r32 = Q.QubitRegister(n, seed=1, precision="fp32")
         setup(r32)
         t = timed(r32)
@@ -826,7 +827,7 @@ def learned_config(n: int, depth: int, seed: int, model: str | None) -> dict:
                      "max_abs_amplitude_error": d.value}
         r32.close()
     r64.close()
-    best = min(("greedy3", "greedy5"), key=lambda k: res[k]["seconds"])
+    best = min(("greedy3", "greedy4", "greedy5"), key=lambda k: res[k]["seconds"])
     return {"workload": f"layered random circuit, {n} qubits, depth {depth}, 10% controlled rotations, seed "
                         f"{9001 + seed} (not seen in training)", "gates": len(ops), **res,
             "learned_gain_vs_best_greedy": res[best]["seconds"] / res["learned"]["seconds"], "best_greedy": best}

@@ -240,10 +240,10 @@ enum qcs_option {
 	QCS_OPT_PASSES = 1,          /* 1 (default): gate lists run as shared-memory passes; 0: one kernel per gate */
 	QCS_OPT_FUSION = 2,          /* gate lists fused into dense blocks: 0 off (FP64 default), 1 greedy (FP32
 	                                default), 2 partition chosen by the learned cost model when one is loaded */
-	QCS_OPT_FUSION_MAX_QUBITS = 3, /* largest fused block (1..5; FP64 registers use at most 4).  Default: 5 on FP32
-	                                  registers of 26 or more qubits with the tensor cores on (4- and 5-qubit blocks
-	                                  on tcgen05 beat blocks of at most 3 on the CUDA cores there), else 3; the
-	                                  learned partition chooses per gate list */
+	QCS_OPT_FUSION_MAX_QUBITS = 3, /* largest fused block (1..5; FP64 registers use at most 4).  Default: 4 on FP32
+	                                  registers of 26 or more qubits with the tensor cores on (4-qubit blocks on
+	                                  tcgen05 beat 5-qubit ones and blocks of at most 3 on the CUDA cores there),
+	                                  else 3; the learned partition chooses per gate list */
 	QCS_OPT_TENSOR_CORES = 4       /* FP32 registers: 1 (default) fused blocks of 4 and 5 qubits run as 3xTF32
 	                                  products on the tensor cores (tcgen05); 0: FP32 FMAs on the CUDA cores */
 };

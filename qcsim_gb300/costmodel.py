@@ -236,6 +236,88 @@ def time_blocks(samples, reps: int = 3, seed: int = 0, log=print) -> tuple[np.nd
     return np.array(X, dtype=np.float32), np.array(T, dtype=np.float32), pass_ms, pass_ms_tc
 
 
+def partition_features(n: int, recs: np.ndarray, max_qubits: int) -> tuple[np.ndarray, int]:
+    """the greedy partition with blocks of at most max_qubits, as the engine scores it in fusion mode 2:
+    the features of its blocks (in tensor-core passes, which run when a block has 4 or more qubits, a
+    smaller block counts as the 4-qubit block it is widened to, with the lowest qubits it lacks) and the
+    number of shared-memory passes it packs into"""
+    plan = fusion_plan(n, recs, max_qubits)
+    tc = n >= 12 and any(bin(m).count("1") >= 4 for m, _ in plan)
+    X = []
+    for mask, ng in plan:
+        q = [b for b in range(n) if (mask >> b) & 1]
+        b = 0
+        while tc and len(q) < 4:
+            if b not in q:
+                q.append(b)
+            b += 1
+        X.append(features(n, sorted(q), ng))
+    pob = fusion_passes(n, recs, max_qubits, 12 if tc else 13, tc)
+    return np.array(X, dtype=np.float32).reshape(-1, F), (max(pob) + 1 if pob else 0)
+
+
+def calibration_runs(count: int, seed: int, log=print) -> list:
+    """device time of whole fused gate lists: `count` seeded layered circuits (24-32 qubits, depth 6-16,
+    10% controlled rotations), each run with the greedy partitions of largest block 1..5.  Returns
+    (block features, passes, n, milliseconds) per run."""
+    import torch
+    from . import circuits as Cc, gates as G
+    from .register import QubitRegister
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(count):
+        n = int(rng.integers(24, 33))
+        depth = int(rng.integers(6, 17))
+        recs = G.records(Cc.layered_circuit(n, depth, seed=seed * 7919 + i, p3=0.02, controlled_frac=0.1))
+        for mq in range(1, 6):
+            X, npass = partition_features(n, recs, mq)
+            reg = QubitRegister(n, seed=1, precision="fp32")
+            reg.set_fusion(1, mq)
+            reg.profile(True)
+            reg.apply_records(recs)  # first touch and planning structures
+            reg.read_profile()
+            reg.apply_records(recs)
+            prof = reg.read_profile()
+            reg.close()
+            torch.cuda.synchronize()
+            ms = sum(v[1] for k, v in prof.items() if k.startswith("tile_pass"))
+            out.append((X, npass, n, ms))
+        log(f"calibration circuit {i}: {n} qubits, depth {depth}: " + ", ".join(f"{r[3]:.2f}" for r in out[-5:]) + " ms")
+    return out
+
+
+def calibrate(mlp: Mlp, pass_ms: dict, runs: list, rounds: int = 4, steps: int = 1500, lr: float = 1e-3,
+              per_run: int = 96, seed: int = 0) -> dict:
+    """fit the block costs to whole-list timings: a list's time beyond its passes' streaming cost,
+    t - passes x pass_ms[n], is shared among its blocks in proportion to the model's current predictions,
+    and the model is trained on those shares; repeated `rounds` times.  Block costs measured one block
+    per pass miss how blocks that share a pass add up; this step fits the sum the partition choice
+    compares.  Returns the mean absolute log error of the predicted list times before and after."""
+    rng = np.random.default_rng(seed)
+
+    def list_error() -> float:
+        err = []
+        for X, npass, n, ms in runs:
+            pred = float(np.exp(mlp.predict(X)).sum()) + npass * pass_ms[n] if len(X) else npass * pass_ms[n]
+            err.append(abs(math.log(pred / ms)))
+        return float(np.mean(err))
+
+    before = list_error()
+    for _ in range(rounds):
+        xs, ts = [], []
+        for X, npass, n, ms in runs:
+            if not len(X):
+                continue
+            p = np.exp(mlp.predict(X)).astype(np.float64)
+            resid = max(ms - npass * pass_ms[n], 0.05 * ms)
+            share = p * (resid / p.sum())
+            idx = rng.permutation(len(X))[:per_run]
+            xs.append(X[idx])
+            ts.append(np.log(share[idx]).astype(np.float32))
+        mlp.train(np.concatenate(xs), np.concatenate(ts), steps=steps, lr=lr)
+    return {"list_log_error_before": before, "list_log_error_after": list_error()}
+
+
 def save(mlp: Mlp, pass_ms: dict, path: Path | None = None, meta: dict | None = None, pass_ms_tc: dict | None = None) -> Path:
     """the parameters and a 128-entry table: [n] = one CUDA-core pass over n qubits, [64 + n] = one
     tensor-core pass (0 where not measured)"""
@@ -293,6 +375,7 @@ def _main() -> None:
     ap.add_argument("--timed", type=int, default=2400, help="distinct blocks timed on the GPU")
     ap.add_argument("--seed", type=int, default=7)
     ap.add_argument("--out", default=str(MODEL_DIR / "fusion_cost_mlp.npz"))
+    ap.add_argument("--calibrate", type=int, default=60, help="circuits timed whole for the calibration step (0: none)")
     args = ap.parse_args()
     t0 = time.time()
     samples = sample_blocks(args.circuits, args.seed)
@@ -316,6 +399,10 @@ def _main() -> None:
     X, T, pass_ms, pass_ms_tc = time_blocks(chosen)
     t2 = time.time()
     mlp, metrics = train_from_timings(X, T)
+    if args.calibrate:
+        runs = calibration_runs(args.calibrate, args.seed)
+        metrics.update(calibrate(mlp, pass_ms, runs))
+        metrics["calibration_runs"] = len(runs)
     t3 = time.time()
     metrics.update({"circuits": args.circuits, "blocks_sampled": len(samples), "distinct_blocks": len(distinct),
                     "blocks_timed": len(chosen), "seconds_sampling": t1 - t0, "seconds_timing": t2 - t1,

@@ -105,11 +105,12 @@ struct qcs_register {
 	// stored values (amplitude / scale) stay far inside the precision's range
 	double scale_limit() const { return prec == QCS_FP64 ? 1e100 : 1e15; }
 	size_t state_bytes() const { return static_cast<size_t>(N) * amp_bytes(); }
-	// the largest fused block: the option when set; otherwise 5 for FP32 registers of at least 26 qubits
-	// with the tensor cores on (their tensor-core passes beat smaller blocks on the CUDA cores there), else 3
+	// the largest fused block: the option when set; otherwise 4 for FP32 registers of at least 26 qubits
+	// with the tensor cores on (tensor-core passes of 4-qubit blocks were the fastest greedy partitions
+	// there, ahead of 5-qubit blocks and of blocks of at most 3 on the CUDA cores), else 3
 	int fusion_limit() const {
 		if (fusion_max > 0) return fusion_max;
-		return prec == QCS_FP32 && tensor_cores && n >= 26 ? 5 : 3;
+		return prec == QCS_FP32 && tensor_cores && n >= 26 ? 4 : 3;
 	}
 };
 

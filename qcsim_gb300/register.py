@@ -87,7 +87,7 @@ class QubitRegister:
 
     def set_fusion(self, mode: int, max_qubits: int | None = None) -> None:
         """fuse gate lists into dense blocks: 0 off, 1 greedy, 2 learned partition (FP32 default: 1, blocks of at
-        most 5 qubits from 26 qubits up with the tensor cores on, else at most 3)"""
+        most 4 qubits from 26 qubits up with the tensor cores on, else at most 3)"""
         self._ck(self._lib.qcs_set_option(self._h, L.QCS_OPT_FUSION, int(mode)))
         if max_qubits is not None:
             self._ck(self._lib.qcs_set_option(self._h, L.QCS_OPT_FUSION_MAX_QUBITS, int(max_qubits)))

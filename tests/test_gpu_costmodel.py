@@ -93,15 +93,15 @@ def test_apply_matrix_any_order(cm):
 
 
 LEARNED_MARGIN = 0.98  # the learned partition's time must be at most this fraction of greedy <=3's
-BEST_SLACK = 1.15      # ... and at most this multiple of the faster greedy fuser's
+BEST_SLACK = 1.15      # ... and at most this multiple of the fastest greedy partition's
 
 
 def test_trained_model_beats_the_fixed_fuser(cm):
     """the committed, GPU-trained cost model against the method without it, on an unseen 26-qubit circuit
     of depth 12 with 10% controlled rotations: the learned partition must take at most LEARNED_MARGIN of
-    the time of greedy blocks of at most 3 qubits on the CUDA cores, and at most BEST_SLACK of the faster
-    greedy fuser's (blocks of at most 5 qubits on the tensor cores run faster still here; the model picks
-    4-qubit blocks); every FP32 result stays within 1-F <= 1e-6 of the FP64 path."""
+    the time of greedy blocks of at most 3 qubits on the CUDA cores, and at most BEST_SLACK of the fastest
+    greedy partition (largest block 3, 4 or 5, found here by timing all three, which the model does not
+    do); every FP32 result stays within 1-F <= 1e-6 of the FP64 path."""
     import ctypes as C
     import torch
     from qcsim_gb300 import QubitRegister, _lib as L, circuits, gates as G
@@ -133,10 +133,11 @@ def test_trained_model_beats_the_fixed_fuser(cm):
         return best, 1.0 - f.value
 
     t_greedy5, inf_greedy5 = run(lambda r: r.set_fusion(1, 5))
+    t_greedy4, inf_greedy4 = run(lambda r: r.set_fusion(1, 4))
     t_greedy3, inf_greedy3 = run(lambda r: r.set_fusion(1, 3))
     t_learned, inf_learned = run(lambda r: cm.attach(r, mlp, pass_ms))
-    assert max(inf_greedy5, inf_greedy3, inf_learned) <= 1e-6
-    t_best = min(t_greedy3, t_greedy5)
-    print(f"learned {t_learned:.2f} ms, greedy<=3 {t_greedy3:.2f} ms, greedy<=5 {t_greedy5:.2f} ms")
+    assert max(inf_greedy5, inf_greedy4, inf_greedy3, inf_learned) <= 1e-6
+    t_best = min(t_greedy3, t_greedy4, t_greedy5)
+    print(f"learned {t_learned:.2f} ms, greedy<=3 {t_greedy3:.2f} ms, greedy<=4 {t_greedy4:.2f} ms, greedy<=5 {t_greedy5:.2f} ms")
     assert t_learned <= LEARNED_MARGIN * t_greedy3, (t_learned, t_greedy3, t_greedy5)
     assert t_learned <= BEST_SLACK * t_best, (t_learned, t_greedy3, t_greedy5)

@@ -172,16 +172,19 @@ def test_block_features_layout():
 
 def test_committed_cost_model_is_sane():
     """the GPU-trained cost model shipped with the package: its parameters load, the CPU restatement of
-    the network predicts finite block times, a 5-qubit block costs more than a 1-qubit block, and the
-    per-size pass times double with each qubit"""
+    the network predicts finite block times, a 5-qubit block of six gates costs less per gate than a
+    one-gate 1-qubit block, the same block costs more on 30 than on 26 qubits, and the per-size pass
+    times (CUDA-core and tensor-core) double with each qubit"""
     from qcsim_gb300 import costmodel as cm
     d = np.load(cm.MODEL_DIR / "fusion_cost_mlp.npz")
     ref = cm.MlpRef(d["params"].astype(np.float64))
-    x = np.stack([cm.features(30, [3], 1), cm.features(30, [2, 7, 11, 20, 29], 6)]).astype(np.float64)
-    y = ref.forward(x).reshape(-1)
-    assert np.all(np.isfinite(y)) and y[1] > y[0]
+    x = np.stack([cm.features(30, [3], 1), cm.features(30, [2, 7, 11, 20, 29], 6),
+                  cm.features(26, [2, 7, 11, 20, 25], 6)]).astype(np.float64)
+    y = np.exp(ref.forward(x).reshape(-1))
+    assert np.all(np.isfinite(y)) and y[1] / 6 < y[0] and y[1] > y[2]
     pm = d["pass_ms"]
     assert all(1.6 < pm[n + 1] / pm[n] < 2.4 for n in range(24, 32))
+    assert all(1.6 < pm[64 + n + 1] / pm[64 + n] < 2.4 for n in range(24, 32))
 
 
 def test_records_match_to_record():
