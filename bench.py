@@ -324,11 +324,11 @@ def parity_at_size(n: int, seed: int, ref_reg, sample, kind: str, shots: int = 1
 
 def small_config_both(seed: int) -> dict:
     """the 20-qubit layered circuit of depth 40 (the CPU-sized configuration) end to end on the GPU
-    (one ApplyGates call, state resident) and on the CPU oracle with every host thread"""
+    (one ApplyGates call, state resident) and on the CPU reference (QCSim's register where its sources
+    are staged, else the oracle's restatement) with every host thread"""
     import torch
     import qcsim_gb300 as Q
     from qcsim_gb300 import circuits, gates as G
-    from oracle import bind
     ops = circuits.layered_circuit(20, 40, seed=seed)
     recs = G.records(ops)
     reg = Q.QubitRegister(20, seed=seed)
@@ -341,16 +341,14 @@ def small_config_both(seed: int) -> dict:
     gpu_s = time.perf_counter() - t0
     gpu_state = reg.getRegisterStorage()
     reg.close()
-    bind.build_oracle()
-    lib = bind.oracle()
-    lib.qo_set_threads(os.cpu_count() or 1)
-    ref = bind.OracleRegister(20)
+    kind, make, threads = reference_cpu()
+    ref = make(20, seed)
     t0 = time.perf_counter()
     ref.apply(ops)
     cpu_s = time.perf_counter() - t0
-    err = float(np.abs(gpu_state - ref.state()).max())
+    err = max_abs_diff(gpu_state, ref.state())
     return {"workload": f"layered random circuit, 20 qubits, depth 40, seed {seed} ({len(ops)} gates)",
-            "gpu_seconds": gpu_s, "cpu_seconds": cpu_s, "cpu_cores": lib.qo_max_threads(), "gpu_gates_per_s": len(ops) / gpu_s,
+            "gpu_seconds": gpu_s, "cpu_seconds": cpu_s, "cpu_kind": kind, "cpu_cores": threads, "gpu_gates_per_s": len(ops) / gpu_s,
             "cpu_gates_per_s": len(ops) / cpu_s, "max_abs_amplitude_difference": err}
 
 
