@@ -16,7 +16,8 @@ namespace qcs {
 // DenseTC: a fused 4- or 5-qubit block (FP32 registers) on the tensor cores; ins = its local positions,
 // mat = offset (complex entries, even) of its real-expanded 2D x 2D matrix as two TF32 splits in the
 // K-major operand layout (hi then lo, 16 D^2 bytes each), lbit1 = its byte offset in the kernel's
-// resident matrix area
+// resident matrix area, gtbit = the tile positions that make up the row (tensor-memory lane) index,
+// 4 bits each, row bit r in bits 4r..4r+3
 // TableDiag: every amplitude of the tile times its entry of a 2^n-entry diagonal on the device (the
 // table's address in gtbit); no inserted positions
 enum class TKind : uint8_t { Ctrl1q = 0, Swap = 1, Dense2 = 2, Dense3 = 3, GlobalDiag = 4, DenseN = 5, PhaseRow = 6, DenseTC = 7,
