@@ -345,7 +345,7 @@ int run_planned(qcs_handle h, const std::vector<PlannedPass>& passes, int kmax, 
 		// a tensor-core pass: FP32, a fused gate list with a block of 4 or 5 qubits (apply_blocks), a 12-qubit
 		// tile, and nothing but fused blocks (smaller ones are widened to 4 qubits); every operation of it
 		// runs on the tensor cores
-		bool tc_pass = tensor_passes && sizeof(T) == 4 && h->tensor_cores && tp.k == kTcTileQubits && L >= 5 && tp.k - L <= 8 &&
+		bool tc_pass = tensor_passes && sizeof(T) == 4 && h->tensor_cores && tp.k == kTcTileQubits && L >= kMinLowRun && tp.k - L <= kMaxHigh &&
 		               !pp.gates.empty();
 		for (const CompiledGate& c : pp.gates) tc_pass = tc_pass && c.kind == GKind::Block && !c.block_q.empty();
 		for (const CompiledGate& c : pp.gates) {
@@ -494,7 +494,7 @@ int run_planned(qcs_handle h, const std::vector<PlannedPass>& passes, int kmax, 
 	}
 	// every index a kernel will form stays inside its tile and every matrix read inside the table
 	for (const TilePass& tp : tps) {
-		if (tp.k < 1 || tp.k > tile_qubits<T>() || tp.L > tp.k || tp.k - tp.L > 8 || tp.nfixed + tp.k != n) {
+		if (tp.k < 1 || tp.k > tile_qubits<T>() || tp.L > tp.k || tp.k - tp.L > kMaxHigh || tp.nfixed + tp.k != n) {
 			h->err = "apply gates: internal error (tile geometry)";
 			return QCS_CUDA_ERROR;
 		}
@@ -579,7 +579,7 @@ int apply_blocks(qcs_handle h, std::vector<FusedBlock> blocks) {
 	for (const FusedBlock& b : blocks) big = big || b.qubits.size() >= 4;
 	const bool tc = h->prec == QCS_FP32 && h->tensor_cores && big;
 	const int kmax = std::min(tc ? kTcTileQubits : (h->prec == QCS_FP64 ? tile_qubits<double>() : tile_qubits<float>()), n);
-	const int L0 = std::min(n, std::max(5, kmax - 8));
+	const int L0 = low_run_qubits(n, kmax);
 	for (const FusedBlock& b : blocks)
 		if (b.qubits.empty()) h->scale *= b.M[0];  // a global factor only
 	std::vector<PlannedPass> passes;
@@ -615,7 +615,7 @@ int fused_apply(qcs_handle h, const qcs_gate* gates, size_t count) {
 	if (h->fusion == 2 && h->cost_ctx) {
 		// the non-tensor-core tile; candidates with tensor-core blocks use kTcTileQubits (costmodel.cu)
 		const int kmax = std::min(h->prec == QCS_FP64 ? tile_qubits<double>() : tile_qubits<float>(), n);
-		const int L0 = std::min(n, std::max(5, kmax - 8));
+		const int L0 = low_run_qubits(n, kmax);
 		const int st = choose_partition(h, cg, kmax, L0, blocks, &h->last_predicted_ms);
 		if (st != QCS_OK) return st;
 	} else {
@@ -638,7 +638,7 @@ namespace {
 constexpr size_t kGateWindow = 64;
 
 int plan_and_run(qcs_handle h, const std::vector<CompiledGate>& cg, int kmax) {
-	const int L0 = std::max(5, kmax - 8);
+	const int L0 = low_run_qubits(static_cast<int>(h->n), kmax);
 	const uint64_t low = (1ULL << L0) - 1;
 	std::vector<PlannedPass> passes;
 	std::vector<char> placed(cg.size(), 0);

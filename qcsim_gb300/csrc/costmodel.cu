@@ -160,7 +160,7 @@ int qcs_fusion_passes(uint32_t nqubits, const qcs_gate* gates, size_t count, int
 	for (qcs::FusedBlock& b : blocks)
 		if (!b.qubits.empty()) real.push_back(std::move(b));
 	const int kmax = std::min(tile_qubits, static_cast<int>(nqubits));
-	const int L0 = std::min(static_cast<int>(nqubits), std::max(5, kmax - 8));
+	const int L0 = qcs::low_run_qubits(static_cast<int>(nqubits), kmax);
 	const auto passes = qcs::pack_blocks(real, kmax, L0, tensor_cores ? qcs::kTcMatBudget : 0u);
 	if (pass_of_block)
 		for (size_t p = 0; p < passes.size(); ++p)

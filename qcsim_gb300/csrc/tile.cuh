@@ -4,6 +4,8 @@
 // and written as contiguous runs of 2^L amplitudes.
 #pragma once
 
+#include <algorithm>
+
 #include "engine.cuh"
 
 namespace qcs {
@@ -22,6 +24,13 @@ namespace qcs {
 // table's address in gtbit); no inserted positions
 enum class TKind : uint8_t { Ctrl1q = 0, Swap = 1, Dense2 = 2, Dense3 = 3, GlobalDiag = 4, DenseN = 5, PhaseRow = 6, DenseTC = 7,
                              TableDiag = 8 };
+
+// every pass's tile holds qubits 0..L0-1, so that a tile moves between HBM and shared memory in runs of
+// 2^L0 contiguous amplitudes (at least 128 bytes, a whole cache line); at most kMaxHigh tile qubits lie
+// above the run.  The fewer qubits the run pins, the more gates or blocks one pass takes.
+constexpr int kMinLowRun = 4;
+constexpr int kMaxHigh = 8;
+inline int low_run_qubits(int n, int kmax) { return std::min(n, std::max(kMinLowRun, kmax - kMaxHigh)); }
 
 // tensor-core passes: tiles of exactly kTcTileQubits qubits; resident block matrices per pass
 constexpr int kTcTileQubits = 12;

@@ -14,7 +14,6 @@ namespace {
 constexpr int kTileThreads = 512;
 // tile loads in flight per thread (FP64 passes are FP64-pipe bound and keep their registers for occupancy)
 template <typename T> constexpr int load_batch() { return sizeof(T) == 4 ? 8 : 1; }
-constexpr int kMaxHigh = 8;  // at most 8 tile qubits above the contiguous low block
 
 // the loop-invariant fields of a TileOp, held in registers
 struct OpRegs {
@@ -379,7 +378,7 @@ __global__ void __launch_bounds__(THREADS) k_tile(cplx_t<T>* __restrict__ s, Til
 	__syncthreads();
 	for (uint64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
 		const uint64_t base = fixed_base(fixtab, tile);
-		// asynchronous 16-byte copies (one FP64 or two FP32 amplitudes, inside one run of 2^L >= 32),
+		// asynchronous 16-byte copies (one FP64 or two FP32 amplitudes, inside one run of 2^L >= 16),
 		// all in flight at once without holding registers
 		constexpr uint32_t kPer = 16 / sizeof(cplx_t<T>);
 		for (uint32_t j = threadIdx.x * kPer; j < K; j += blockDim.x * kPer)
@@ -711,7 +710,7 @@ cudaError_t launch_tile_pass(cplx_t<T>* s, const TilePass& p, const TileOp* d_op
 				}
 			}
 			const size_t smem = kTcSmem + static_cast<size_t>(p.op_count) * (sizeof(TileOp) + sizeof(TcTab));
-			if (p.k != kTcTileQubits || p.L < 5 || p.k - p.L > kMaxHigh || p.nfixed > 8 * kFixChunks || !d_err ||
+			if (p.k != kTcTileQubits || p.L < kMinLowRun || p.k - p.L > kMaxHigh || p.nfixed > 8 * kFixChunks || !d_err ||
 			    smem > kTcSmemLimit)
 				return cudaErrorInvalidValue;
 			const uint64_t ntiles = 1ULL << p.nfixed;

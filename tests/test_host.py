@@ -140,7 +140,7 @@ def test_pass_packing_respects_order_and_tiles():
         plan = costmodel.fusion_plan(n, recs, mq)
         passes = costmodel.fusion_passes(n, recs, mq, k, tc)
         assert len(passes) == len(plan)
-        low = (1 << min(n, max(5, k - 8))) - 1
+        low = (1 << min(n, max(4, k - 8))) - 1  # the low run every tile holds (tile.cuh low_run_qubits)
         union: dict[int, int] = {}
         for (mask, _), p in zip(plan, passes):
             union[p] = union.get(p, low) | mask
