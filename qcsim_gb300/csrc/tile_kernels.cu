@@ -539,8 +539,7 @@ __device__ bool tc_block(float2* sm, const TcTab& tab, const unsigned char* sBop
 #pragma unroll
 	for (uint32_t c8 = 0; c8 < 2; ++c8) {
 		float v[16], w[16];
-		tc::tmem_ld16(tmem + lanes + acc + 16u * c8, v);
-		tc::tmem_ld16(tmem + lanes + hilo + 16u * c8, w);
+		tc::tmem_ld16x2(tmem + lanes + acc + 16u * c8, tmem + lanes + hilo + 16u * c8, v, w);
 		const uint32_t base = rb ^ (c8 ? bw[3] : 0u);
 #pragma unroll
 		for (uint32_t u = 0; u < 8; ++u) {
