@@ -487,14 +487,16 @@ __device__ bool tc_block(float2* sm, const TcTab& tab, const unsigned char* sBop
 	const uint32_t a_lo = K == 5 ? kTcAcol + 64u + 32u * h : kTcAcol + 64u * h + 32u;
 	const uint32_t acc = K == 5 ? 32u * h : 64u * h;
 	const uint32_t hilo = K == 5 ? 64u + 32u * h : 64u * h + 32u;
+	float2 av[16];
+#pragma unroll
+	for (uint32_t u = 0; u < 16; ++u)
+		av[u] = sm[rb ^ ((u & 1u) ? bw[0] : 0u) ^ ((u & 2u) ? bw[1] : 0u) ^ ((u & 4u) ? bw[2] : 0u) ^ ((u & 8u) ? bw[3] : 0u)];
 #pragma unroll
 	for (uint32_t c8 = 0; c8 < 2; ++c8) {
-		const uint32_t base = rb ^ (c8 ? bw[3] : 0u);
 		float hi[16], lo[16];
 #pragma unroll
 		for (uint32_t u = 0; u < 8; ++u) {
-			const uint32_t off = base ^ ((u & 1u) ? bw[0] : 0u) ^ ((u & 2u) ? bw[1] : 0u) ^ ((u & 4u) ? bw[2] : 0u);
-			const float2 v = sm[off];
+			const float2 v = av[8 * c8 + u];
 			const float hx = tf32_rna(v.x), hy = tf32_rna(v.y);
 			hi[2 * u] = hx;
 			hi[2 * u + 1] = hy;
