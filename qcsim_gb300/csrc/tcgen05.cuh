@@ -29,6 +29,12 @@ __host__ __device__ constexpr uint32_t idesc_tf32(uint32_t m, uint32_t n) {
 	return (1u << 4) | (2u << 7) | (2u << 10) | ((n >> 3) << 17) | ((m >> 4) << 24);
 }
 
+// x rounded to TF32 (10 mantissa bits), to nearest with ties away from zero: half a TF32 unit added to the
+// magnitude bits, the 13 low bits cleared.  For finite x of magnitude below 2^128 - 2^116 the same value as
+// cvt.rna.tf32.f32 (tests/tf32_rounding_check.cu compares the two on every such input), in two integer
+// instructions instead of a conversion, whose lower throughput bounded the tensor-core operand gather.
+__device__ __forceinline__ float tf32_rna(float x) { return __uint_as_float((__float_as_uint(x) + 0x1000u) & 0xFFFFE000u); }
+
 __device__ __forceinline__ uint32_t smem_addr(const void* p) { return static_cast<uint32_t>(__cvta_generic_to_shared(p)); }
 
 // whole warp: allocate `ncols` tensor-memory columns, address written to *slot

@@ -440,11 +440,6 @@ constexpr uint32_t kTcWaitTries = 1u << 22;
 constexpr int kTcLoads = (1 << kTcTileQubits) / kTcThreads;  // 16 amplitudes per thread and tile
 static_assert(kTcThreads == 256 && kTcTileQubits == 12, "tile index = thread + 256 i");
 
-// x rounded to TF32 (10 mantissa bits), to nearest with ties away from zero, for finite x: half a TF32 unit
-// added to the magnitude bits, the 13 low bits cleared.  The same values as cvt.rna.tf32.f32, in two integer
-// instructions instead of a conversion (the conversion's lower throughput bounded the operand gather).
-__device__ __forceinline__ float tf32_rna(float x) { return __uint_as_float((__float_as_uint(x) + 0x1000u) & 0xFFFFE000u); }
-
 // swizzled offset of tile index x (XOR of the offsets of its set bits)
 __host__ __device__ constexpr uint32_t tc_offset(uint32_t x) {
 	uint32_t o = 0;
@@ -497,7 +492,7 @@ __device__ bool tc_block(float2* sm, const TcTab& tab, const unsigned char* sBop
 #pragma unroll
 		for (uint32_t u = 0; u < 8; ++u) {
 			const float2 v = av[8 * c8 + u];
-			const float hx = tf32_rna(v.x), hy = tf32_rna(v.y);
+			const float hx = tc::tf32_rna(v.x), hy = tc::tf32_rna(v.y);
 			hi[2 * u] = hx;
 			hi[2 * u + 1] = hy;
 			lo[2 * u] = v.x - hx;  // exact; the tensor core reads it as TF32
