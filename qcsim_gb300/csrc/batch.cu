@@ -228,6 +228,8 @@ bool op_in_bounds(const TileOp& op, int k, size_t mats) {
 		if (rows != (((1u << kTcTileQubits) - 1) & ~insmask) || (op.gtbit >> (4 * (kTcTileQubits - op.nins))) != 0) return false;
 		return op.mat + size_t(4) * D * D <= mats;
 	}
+	if (static_cast<TKind>(op.kind) == TKind::TileFactor)  // one scalar per tile: entries mat and mat + 1
+		return op.nins == 0 && op.lset == 0 && op.gtbit != 0 && (op.gtbit & (op.gtbit - 1)) == 0 && op.mat + 2 <= mats;
 	if (static_cast<TKind>(op.kind) == TKind::TableDiag)  // every amplitude of the tile, from the table at gtbit
 		return op.nins == 0 && op.lset == 0 && op.gmask == 0 && op.gtbit != 0 && (op.gtbit & 15u) == 0;
 	if (static_cast<TKind>(op.kind) == TKind::PhaseRow) {
@@ -283,6 +285,18 @@ double fp_ops_per_item(const TileOp& op) {
 // (non-tile controls halve the tiles each; a non-tile phase target runs in half of them)
 double pass_fp_ops(const TilePass& tp, const std::vector<TileOp>& ops, int n) {
 	double total = 0;
+	if (tp.nfactor) {
+		// the TileFactor product multiplies the tiles where it is not one (one complex product per amplitude);
+		// the fraction of such tiles is estimated as if the operations' bits were independent
+		double one = 1.0;
+		for (uint32_t i = tp.op_begin; i < tp.op_begin + tp.nfactor; ++i) {
+			const TileOp& op = ops[i];
+			const double applies = std::ldexp(1.0, -popcount64(op.gmask));
+			const bool both = op.pad[0] != 0;  // a diagonal with two non-unit entries
+			one *= 1.0 - applies * (both ? 1.0 : 0.5);
+		}
+		total += 4.0 * std::ldexp(1.0, n) * (1.0 - one);
+	}
 	for (uint32_t i = tp.op_begin; i < tp.op_begin + tp.op_count; ++i) {
 		const TileOp& op = ops[i];
 		double tiles = std::ldexp(1.0, n - tp.k - popcount64(op.gmask));
@@ -459,6 +473,36 @@ int run_planned(qcs_handle h, const std::vector<PlannedPass>& passes, int kmax, 
 			for (size_t i = 0; i < ins.size(); ++i) op.ins |= static_cast<uint64_t>(ins[i]) << (8 * i);
 			ops.push_back(op);
 		}
+		// diagonal gates whose target and controls all lie outside the tile (Diag and Phase forms) each scale a
+		// whole tile by one factor, so they commute with every other operation of the pass: with two or more,
+		// they become TileFactor operations at the front of the pass, whose product the kernel applies as it
+		// stores the tile
+		if (!tc_pass) {
+			std::vector<TileOp> front, rest;
+			for (size_t i = tp.op_begin; i < ops.size(); ++i) {
+				const TileOp& op = ops[i];
+				const bool merge = static_cast<TKind>(op.kind) == TKind::GlobalDiag && op.lset == 0 && op.nins == 0 &&
+				                   (static_cast<Op1>(op.op) == Op1::Diag || static_cast<Op1>(op.op) == Op1::Phase);
+				(merge ? front : rest).push_back(op);
+			}
+			if (front.size() >= 2) {
+				for (TileOp& op : front) {
+					const bool diag = static_cast<Op1>(op.op) == Op1::Diag;
+					const bool flag = op.lbit0 != 0;  // a phase acts where the target bit equals it
+					const cplx_t<T> one = mk_host<T>(1.0, 0.0), m00 = mats[op.mat], m11 = mats[op.mat + 3];
+					mats[op.mat] = diag ? m00 : (flag ? one : m11);
+					mats[op.mat + 1] = diag ? m11 : (flag ? m11 : one);
+					op.kind = static_cast<uint8_t>(TKind::TileFactor);
+					op.op = 0;
+					op.lbit0 = 0;
+					op.pad[0] = diag ? 1 : 0;
+				}
+				ops.resize(tp.op_begin);
+				ops.insert(ops.end(), front.begin(), front.end());
+				ops.insert(ops.end(), rest.begin(), rest.end());
+				tp.nfactor = static_cast<uint32_t>(front.size());
+			}
+		}
 		tp.op_count = static_cast<uint32_t>(ops.size()) - tp.op_begin;
 		tps.push_back(tp);
 	}
@@ -494,10 +538,16 @@ int run_planned(qcs_handle h, const std::vector<PlannedPass>& passes, int kmax, 
 	}
 	// every index a kernel will form stays inside its tile and every matrix read inside the table
 	for (const TilePass& tp : tps) {
-		if (tp.k < 1 || tp.k > tile_qubits<T>() || tp.L > tp.k || tp.k - tp.L > kMaxHigh || tp.nfixed + tp.k != n) {
+		if (tp.k < 1 || tp.k > tile_qubits<T>() || tp.L > tp.k || tp.k - tp.L > kMaxHigh || tp.nfixed + tp.k != n ||
+		    tp.nfactor > tp.op_count) {
 			h->err = "apply gates: internal error (tile geometry)";
 			return QCS_CUDA_ERROR;
 		}
+		for (uint32_t i = tp.op_begin; i < tp.op_begin + tp.op_count; ++i)
+			if ((static_cast<TKind>(ops[i].kind) == TKind::TileFactor) != (i < tp.op_begin + tp.nfactor)) {
+				h->err = "apply gates: internal error (tile factor order)";
+				return QCS_CUDA_ERROR;
+			}
 		for (uint32_t i = tp.op_begin; i < tp.op_begin + tp.op_count; ++i)
 			if (!op_in_bounds(ops[i], tp.k, mats.size()) || (tp.dense == 2) != (static_cast<TKind>(ops[i].kind) == TKind::DenseTC) ||
 			    (static_cast<TKind>(ops[i].kind) == TKind::PhaseRow && ops[i].pad[4] &&

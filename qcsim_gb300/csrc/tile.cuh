@@ -22,8 +22,12 @@ namespace qcs {
 // 4 bits each, row bit r in bits 4r..4r+3
 // TableDiag: every amplitude of the tile times its entry of a 2^n-entry diagonal on the device (the
 // table's address in gtbit); no inserted positions
+// TileFactor: a diagonal gate whose target (gtbit) and controls (gmask) all lie outside the tile, so that it
+// multiplies each tile by one scalar: mat[0] where the tile's target bit is clear, mat[1] where it is set, in
+// tiles whose fixed bits include gmask.  A pass's TileFactor operations come first (TilePass::nfactor); the
+// kernel multiplies their product into the tile as it stores it, in place of one sweep of the tile per gate.
 enum class TKind : uint8_t { Ctrl1q = 0, Swap = 1, Dense2 = 2, Dense3 = 3, GlobalDiag = 4, DenseN = 5, PhaseRow = 6, DenseTC = 7,
-                             TableDiag = 8 };
+                             TableDiag = 8, TileFactor = 9 };
 
 // every pass's tile holds qubits 0..L0-1, so that a tile moves between HBM and shared memory in runs of
 // 2^L0 contiguous amplitudes (at least 128 bytes, a whole cache line); at most kMaxHigh tile qubits lie
@@ -72,6 +76,7 @@ struct TilePass {
 	uint8_t high[32];      // global positions of local bits L..k-1
 	uint8_t fixed[40];     // global positions of the non-tile qubits, ascending
 	uint32_t op_begin, op_count;
+	uint32_t nfactor;      // the first nfactor operations are TileFactor ones
 	int dense;             // 0: light operations only; 1: dense blocks on the CUDA cores; 2: tensor-core blocks
 	int ops_in_smem;       // set by the launcher: the CTA copies the pass's operations into shared memory
 };

@@ -357,6 +357,7 @@ __global__ void __launch_bounds__(THREADS) k_tile(cplx_t<T>* __restrict__ s, Til
 	extern __shared__ __align__(1024) unsigned char smraw[];
 	__shared__ uint64_t highoff[1 << kMaxHigh];
 	__shared__ uint64_t fixtab[kFixChunks][256];
+	__shared__ cplx_t<T> tile_factor;
 	cplx_t<T>* sm = reinterpret_cast<cplx_t<T>*>(smraw);
 	const uint32_t K = 1u << p.k;
 	build_fix_tables(fixtab, p);
@@ -383,9 +384,18 @@ __global__ void __launch_bounds__(THREADS) k_tile(cplx_t<T>* __restrict__ s, Til
 		constexpr uint32_t kPer = 16 / sizeof(cplx_t<T>);
 		for (uint32_t j = threadIdx.x * kPer; j < K; j += blockDim.x * kPer)
 			tc::cp_async16(sm + j, s + (base | highoff[j >> p.L] | (j & lowmask)));
+		if (threadIdx.x == 0) {
+			// the product of the pass's TileFactor operations for this tile, while the copies are in flight
+			cplx_t<T> f = mk<T>(T(1), T(0));
+			for (uint32_t oi = 0; oi < p.nfactor; ++oi) {
+				const TileOp& op = opsrc[oi];
+				if ((base & op.gmask) == op.gmask) f = cmul<T>(f, mats[op.mat + ((base & op.gtbit) ? 1u : 0u)]);
+			}
+			tile_factor = f;
+		}
 		tc::cp_async_wait_all();
 		__syncthreads();
-		for (uint32_t oi = 0; oi < p.op_count; ++oi) {
+		for (uint32_t oi = p.nfactor; oi < p.op_count; ++oi) {
 			const TileOp op = opsrc[oi];
 			if ((base & op.gmask) != op.gmask) continue;
 			if (static_cast<TKind>(op.kind) == TKind::TableDiag) {
@@ -396,12 +406,14 @@ __global__ void __launch_bounds__(THREADS) k_tile(cplx_t<T>* __restrict__ s, Til
 			}
 			__syncthreads();
 		}
+		const cplx_t<T> f = tile_factor;
+		const bool scaled = f.x != T(1) || f.y != T(0);
 		for (uint32_t j0 = threadIdx.x; j0 < K; j0 += blockDim.x * load_batch<T>()) {
 			cplx_t<T> r[load_batch<T>()];
 #pragma unroll
 			for (int b = 0; b < load_batch<T>(); ++b) {
 				const uint32_t j = j0 + b * blockDim.x;
-				if (j < K) r[b] = sm[j];
+				if (j < K) r[b] = scaled ? cmul<T>(sm[j], f) : sm[j];
 			}
 #pragma unroll
 			for (int b = 0; b < load_batch<T>(); ++b) {

@@ -530,6 +530,47 @@ def test_pass_fp_op_count(Q):
     reg.close()
 
 
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_tile_factors(Q, precision):
+    """diagonal gates whose target and controls all lie outside a pass's tile scale each tile by one factor:
+    a pass with two or more of them applies their product as it stores the tile (TileFactor operations).
+    Here one pass holds H on qubits 0-11 and phases (RZ and P) on qubits 12-17, a CP with a non-tile control
+    and a CZ (a sign flip, kept as its own operation); unfused, so that FP32 runs the same light pass.  The
+    result matches the oracle, and the profile counts one complex product per amplitude for all the
+    non-tile phases together"""
+    from qcsim_gb300 import gates as G
+    n = 18
+    N = 1 << n
+    tile = 12 if precision == "fp64" else 13  # H fixes qubits 0-11; the planner fills the tile from the bottom
+    r = np.random.default_rng(5)
+    ops = [(G.HadamardGate(), q) for q in range(12)]
+    for q in range(12, 18):
+        ops.append((G.RzGate(float(r.uniform(0, 2 * np.pi))), q))
+        ops.append((G.PhaseShiftGate(float(r.uniform(0, 2 * np.pi))), q))
+    ops += [(G.ControlledPhaseShiftGate(0.7), 15, 13), (G.ControlledZGate(), 16, 12)]
+    init = rand_state(n, 9)
+    reg = Q.QubitRegister(n, seed=1, precision=precision)
+    reg.set_fusion(0)
+    reg.setRegisterStorageFastNoNormalize(init)
+    reg.ApplyGates(ops)  # planning warm-up
+    reg.setRegisterStorageFastNoNormalize(init)
+    reg.profile(True)
+    reg.read_profile()
+    reg.ApplyGates(ops)
+    prof = reg.read_profile(fp_ops=True)
+    got = reg.getRegisterStorage()
+    want = oracle_state(n, ops, init)
+    assert np.abs(got - want).max() <= (TOL if precision == "fp64" else 2e-6)
+    launches, _, _, fp = prof["tile_pass"]
+    # 12 factored rotations (2 per amplitude), each phase on a tile qubit one complex product on half the
+    # amplitudes (2 per amplitude), and the factor product on every tile where it is not one
+    local_phases = 2 * (tile - 12)
+    factors = 2 * (18 - tile)
+    want_fp = N * (2 * 12 + 2 * local_phases + 4 * (1 - 0.5 ** factors * 0.75))
+    assert launches == 1 and abs(fp - want_fp) <= 1e-9 * want_fp, (launches, fp, want_fp)
+    reg.close()
+
+
 @pytest.mark.parametrize("batched", [False, True])
 def test_fp32_long_factored_sequences(Q, batched):
     """600 Hadamards on one qubit of an FP32 register (each leaves a factor 1/sqrt(2) pending): the
