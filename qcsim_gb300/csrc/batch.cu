@@ -473,19 +473,22 @@ int run_planned(qcs_handle h, const std::vector<PlannedPass>& passes, int kmax, 
 			for (size_t i = 0; i < ins.size(); ++i) op.ins |= static_cast<uint64_t>(ins[i]) << (8 * i);
 			ops.push_back(op);
 		}
-		// diagonal gates whose target and controls all lie outside the tile (Diag and Phase forms) each scale a
-		// whole tile by one factor, so they commute with every other operation of the pass: with two or more,
-		// they become TileFactor operations at the front of the pass, whose product the kernel applies as it
-		// stores the tile
+		// diagonal gates whose target and controls all lie outside the tile each scale a whole tile by one
+		// factor, so they commute with every other operation of the pass: with two or more of Diag or Phase
+		// form, they become TileFactor operations at the front of the pass, whose product the kernel applies
+		// as it stores the tile; the pass's sign and +-i phases of that kind join them (exact products)
 		if (!tc_pass) {
 			std::vector<TileOp> front, rest;
+			size_t products = 0;
 			for (size_t i = tp.op_begin; i < ops.size(); ++i) {
 				const TileOp& op = ops[i];
+				const Op1 form = static_cast<Op1>(op.op);
 				const bool merge = static_cast<TKind>(op.kind) == TKind::GlobalDiag && op.lset == 0 && op.nins == 0 &&
-				                   (static_cast<Op1>(op.op) == Op1::Diag || static_cast<Op1>(op.op) == Op1::Phase);
+				                   (form == Op1::Diag || form == Op1::Phase || form == Op1::PhaseNeg || form == Op1::PhaseI);
 				(merge ? front : rest).push_back(op);
+				if (merge && (form == Op1::Diag || form == Op1::Phase)) ++products;
 			}
-			if (front.size() >= 2) {
+			if (products >= 2) {
 				for (TileOp& op : front) {
 					const bool diag = static_cast<Op1>(op.op) == Op1::Diag;
 					const bool flag = op.lbit0 != 0;  // a phase acts where the target bit equals it

@@ -535,9 +535,9 @@ def test_tile_factors(Q, precision):
     """diagonal gates whose target and controls all lie outside a pass's tile scale each tile by one factor:
     a pass with two or more of them applies their product as it stores the tile (TileFactor operations).
     Here one pass holds H on qubits 0-11 and phases (RZ and P) on qubits 12-17, a CP with a non-tile control
-    and a CZ (a sign flip, kept as its own operation); unfused, so that FP32 runs the same light pass.  The
-    result matches the oracle, and the profile counts one complex product per amplitude for all the
-    non-tile phases together"""
+    and a CZ (a sign flip: a factor too where both its qubits lie outside the tile); unfused, so that FP32
+    runs the same light pass.  The result matches the oracle, and the profile counts one complex product
+    per amplitude for all the non-tile phases together"""
     from qcsim_gb300 import gates as G
     n = 18
     N = 1 << n
@@ -566,7 +566,8 @@ def test_tile_factors(Q, precision):
     # amplitudes (2 per amplitude), and the factor product on every tile where it is not one
     local_phases = 2 * (tile - 12)
     factors = 2 * (18 - tile)
-    want_fp = N * (2 * 12 + 2 * local_phases + 4 * (1 - 0.5 ** factors * 0.75))
+    cz = 0.75 if tile == 12 else 1.0  # the CZ's control (qubit 12) is a tile qubit in the 13-qubit tile
+    want_fp = N * (2 * 12 + 2 * local_phases + 4 * (1 - 0.5 ** factors * 0.75 * cz))
     assert launches == 1 and abs(fp - want_fp) <= 1e-9 * want_fp, (launches, fp, want_fp)
     reg.close()
 
