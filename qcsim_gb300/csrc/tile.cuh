@@ -24,8 +24,9 @@ namespace qcs {
 // table's address in gtbit); no inserted positions
 // TileFactor: a diagonal gate whose target (gtbit) and controls (gmask) all lie outside the tile, so that it
 // multiplies each tile by one scalar: mat[0] where the tile's target bit is clear, mat[1] where it is set, in
-// tiles whose fixed bits include gmask.  A pass's TileFactor operations come first (TilePass::nfactor); the
-// kernel multiplies their product into the tile as it stores it, in place of one sweep of the tile per gate.
+// tiles whose fixed bits include gmask; pad[0] = 1 when both entries differ from one (instruction counts
+// only).  A pass's TileFactor operations come first (TilePass::nfactor); the kernel multiplies their product
+// into the tile as it stores it, in place of one sweep of the tile per gate.
 enum class TKind : uint8_t { Ctrl1q = 0, Swap = 1, Dense2 = 2, Dense3 = 3, GlobalDiag = 4, DenseN = 5, PhaseRow = 6, DenseTC = 7,
                              TableDiag = 8, TileFactor = 9 };
 
