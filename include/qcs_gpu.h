@@ -231,6 +231,13 @@ int qcs_fusion_plan(uint32_t nqubits, const qcs_gate* gates, size_t count, int m
  * is block i's pass (blocks as numbered by qcs_fusion_plan, global-factor blocks get UINT32_MAX) */
 int qcs_fusion_passes(uint32_t nqubits, const qcs_gate* gates, size_t count, int max_qubits, int tile_qubits, int tensor_cores,
                       uint32_t* pass_of_block, size_t capacity, size_t* nblocks_out, size_t* npasses_out);
+/* the shared-memory passes qcs_apply_gates plans for an unfused gate list on a register of this size and
+ * precision (host only, no GPU): per pass its number of operations and, of those, the TileFactor ones
+ * (diagonal gates outside the pass's tile merged into one factor per tile).  A list that runs one kernel
+ * per gate (fewer than tile + 2 qubits, or a single gate) reports no passes; npasses_out may exceed
+ * capacity (then only capacity entries are written) */
+int qcs_plan_gate_passes(uint32_t nqubits, int precision, const qcs_gate* gates, size_t count, uint32_t* pass_ops,
+                         uint32_t* pass_factors, size_t capacity, size_t* npasses_out);
 /* attach a trained model (kept by the caller) and the measured time of one pass per register size
  * (pass_ms[n], milliseconds; with len >= 128, pass_ms[64 + n] is that of a tensor-core pass); NULL detaches */
 int qcs_set_cost_model(qcs_handle h, qcs_mlp_handle mlp, const double* pass_ms, size_t len);

@@ -123,6 +123,7 @@ SIGNATURES = {
     "qcs_set_cost_model": (_i, [_h, _h, _pd, _sz]),
     "qcs_fusion_plan": (_i, [_u32, C.c_void_p, _sz, _i, C.POINTER(C.c_uint64), C.POINTER(_u32), _sz, C.POINTER(_sz)]),
     "qcs_fusion_passes": (_i, [_u32, C.c_void_p, _sz, _i, _i, _i, C.POINTER(_u32), _sz, C.POINTER(_sz), C.POINTER(_sz)]),
+    "qcs_plan_gate_passes": (_i, [_u32, _i, C.c_void_p, _sz, C.POINTER(_u32), C.POINTER(_u32), _sz, C.POINTER(_sz)]),
     "qcs_set_option": (_i, [_h, _i, _i]),
     "qcs_profile_enable": (_i, [_h, _i]),
     "qcs_profile_read": (_i, [_h, C.c_void_p, _i, C.POINTER(_i)]),

@@ -66,6 +66,21 @@ def fusion_passes(n: int, recs: np.ndarray, max_qubits: int, tile_qubits: int, t
     return out
 
 
+def gate_passes(n: int, recs: np.ndarray, precision: str = "fp64") -> list[tuple[int, int]]:
+    """(operations, TileFactor operations) of each shared-memory pass qcs_apply_gates plans for an unfused
+    gate list (host only)"""
+    lib = L.load()
+    recs = np.ascontiguousarray(recs, dtype=L.GATE_DTYPE)
+    cap = len(recs) + 1
+    nops = np.zeros(cap, dtype=np.uint32)
+    nfac = np.zeros(cap, dtype=np.uint32)
+    npass = C.c_size_t()
+    L.check(lib.qcs_plan_gate_passes(n, L.QCS_FP64 if precision == "fp64" else L.QCS_FP32, recs.ctypes.data_as(C.c_void_p),
+                                     len(recs), nops.ctypes.data_as(C.POINTER(C.c_uint32)),
+                                     nfac.ctypes.data_as(C.POINTER(C.c_uint32)), cap, C.byref(npass)))
+    return [(int(nops[i]), int(nfac[i])) for i in range(min(cap, npass.value))]
+
+
 class Mlp:
     """the engine's MLP (qcs_mlp_*)"""
 

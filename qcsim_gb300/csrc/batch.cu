@@ -306,14 +306,26 @@ double pass_fp_ops(const TilePass& tp, const std::vector<TileOp>& ops, int n) {
 	return total;
 }
 
+// the tiles, operations and matrix table of planned passes, before any device buffer is touched
 template <typename T>
-int run_planned(qcs_handle h, const std::vector<PlannedPass>& passes, int kmax, int L0, bool tensor_passes = false) {
-	const int n = static_cast<int>(h->n);
+struct PassOps {
 	std::vector<TilePass> tps;
 	std::vector<TileOp> ops;
 	std::vector<cplx_t<T>> mats;
+	uint32_t rowM = 0;  // QFT phase rows: bits of the widest row's table of roots, 0 without rows
+};
+
+// builds the passes' operations for a register of n qubits (host only); tensor-core passes only where
+// tensor_passes and tensor_cores are both set; false, with err set, on an internal error
+template <typename T>
+bool build_pass_ops(int n, bool tensor_cores, const std::vector<PlannedPass>& passes, int kmax, int L0, bool tensor_passes,
+                    PassOps<T>& po, std::string& err) {
+	std::vector<TilePass>& tps = po.tps;
+	std::vector<TileOp>& ops = po.ops;
+	std::vector<cplx_t<T>>& mats = po.mats;
 	// QFT phase rows share one pair of tables of 2^M-th roots of unity: hi[u] = w^(u 2^S), lo[v] = w^v
-	uint32_t rowM = 0, rowS = 0, row_tab = 0;
+	uint32_t& rowM = po.rowM;
+	uint32_t rowS = 0, row_tab = 0;
 	for (const PlannedPass& pp : passes)
 		for (const CompiledGate& c : pp.gates)
 			if (c.kind == GKind::PhaseRow) rowM = std::max(rowM, c.row_bits + 1);
@@ -359,7 +371,7 @@ int run_planned(qcs_handle h, const std::vector<PlannedPass>& passes, int kmax, 
 		// a tensor-core pass: FP32, a fused gate list with a block of 4 or 5 qubits (apply_blocks), a 12-qubit
 		// tile, and nothing but fused blocks (smaller ones are widened to 4 qubits); every operation of it
 		// runs on the tensor cores
-		bool tc_pass = tensor_passes && sizeof(T) == 4 && h->tensor_cores && tp.k == kTcTileQubits && L >= kMinLowRun && tp.k - L <= kMaxHigh &&
+		bool tc_pass = tensor_passes && sizeof(T) == 4 && tensor_cores && tp.k == kTcTileQubits && L >= kMinLowRun && tp.k - L <= kMaxHigh &&
 		               !pp.gates.empty();
 		for (const CompiledGate& c : pp.gates) tc_pass = tc_pass && c.kind == GKind::Block && !c.block_q.empty();
 		for (const CompiledGate& c : pp.gates) {
@@ -433,8 +445,8 @@ int run_planned(qcs_handle h, const std::vector<PlannedPass>& passes, int kmax, 
 					if (pos.size() < 4) M = pad_block(pos, M, tp.k);
 					const uint32_t K = static_cast<uint32_t>(pos.size());
 					if (tc_slot + 32u * (1u << (2 * K)) > kTcMatBudget) {
-						h->err = "apply gates: internal error (tensor-core pass over its matrix budget)";
-						return QCS_CUDA_ERROR;
+						err = "apply gates: internal error (tensor-core pass over its matrix budget)";
+						return false;
 					}
 					op.kind = static_cast<uint8_t>(TKind::DenseTC);
 					uint32_t insmask = 0;
@@ -509,6 +521,18 @@ int run_planned(qcs_handle h, const std::vector<PlannedPass>& passes, int kmax, 
 		tp.op_count = static_cast<uint32_t>(ops.size()) - tp.op_begin;
 		tps.push_back(tp);
 	}
+	return true;
+}
+
+template <typename T>
+int run_planned(qcs_handle h, const std::vector<PlannedPass>& passes, int kmax, int L0, bool tensor_passes = false) {
+	const int n = static_cast<int>(h->n);
+	PassOps<T> po;
+	if (!build_pass_ops<T>(n, h->tensor_cores, passes, kmax, L0, tensor_passes, po, h->err)) return QCS_CUDA_ERROR;
+	std::vector<TilePass>& tps = po.tps;
+	std::vector<TileOp>& ops = po.ops;
+	std::vector<cplx_t<T>>& mats = po.mats;
+	const uint32_t rowM = po.rowM;
 	BatchBuffers* bb = static_cast<BatchBuffers*>(h->batch);
 	if (!bb) {
 		bb = new BatchBuffers;
@@ -682,16 +706,15 @@ int fused_apply(qcs_handle h, const qcs_gate* gates, size_t count) {
 
 namespace {
 
-// packs compiled gates into shared-memory passes and runs them.  Each pass takes, in order, every gate
-// whose local qubits fit its tile and which shares no qubit with an earlier gate still waiting
-// (gates on disjoint qubits commute), looking at most kGateWindow gates ahead.  The global factors
-// taken out of the gates multiply into the register's scale in placement order; when its magnitude
-// leaves [1/L, L] (L = qcs_register::scale_limit: 1e100 in FP64, 1e15 in FP32) the pass closes and the
-// scale is folded into the amplitudes after it.
+// packs compiled gates into shared-memory passes (plan_and_run then runs them).  Each pass takes, in
+// order, every gate whose local qubits fit its tile and which shares no qubit with an earlier gate still
+// waiting (gates on disjoint qubits commute), looking at most kGateWindow gates ahead.  The global factors
+// taken out of the gates multiply into `scale` (the register's) in placement order; when its magnitude
+// leaves [1/limit, limit] (scale_limit_of: 1e100 in FP64, 1e15 in FP32) the pass closes and the scale is
+// folded into the amplitudes after it.
 constexpr size_t kGateWindow = 64;
 
-int plan_and_run(qcs_handle h, const std::vector<CompiledGate>& cg, int kmax) {
-	const int L0 = low_run_qubits(static_cast<int>(h->n), kmax);
+std::vector<PlannedPass> place_gates(const std::vector<CompiledGate>& cg, int kmax, int L0, std::complex<double>& scale, double limit) {
 	const uint64_t low = (1ULL << L0) - 1;
 	std::vector<PlannedPass> passes;
 	std::vector<char> placed(cg.size(), 0);
@@ -712,15 +735,15 @@ int plan_and_run(qcs_handle h, const std::vector<CompiledGate>& cg, int kmax) {
 			const bool fits = popcount64(pp.tmask | need) <= kmax;
 			if ((touch & waiting) == 0 && (fits || pp.gates.empty())) {
 				placed[i] = 1;
-				h->scale *= c.scale;
+				scale *= c.scale;
 				if (c.kind != GKind::Identity) {
 					pp.tmask |= need;
 					pp.gates.push_back(c);
 				}
-				const double mag = std::abs(h->scale);
-				if (mag > h->scale_limit() || mag < 1.0 / h->scale_limit()) {
-					pp.fold_after = h->scale;
-					h->scale = std::complex<double>(1.0, 0.0);
+				const double mag = std::abs(scale);
+				if (mag > limit || mag < 1.0 / limit) {
+					pp.fold_after = scale;
+					scale = std::complex<double>(1.0, 0.0);
 					fold = true;
 				}
 			} else {
@@ -733,6 +756,12 @@ int plan_and_run(qcs_handle h, const std::vector<CompiledGate>& cg, int kmax) {
 		passes.emplace_back();
 		passes.back().tmask = low;
 	}
+	return passes;
+}
+
+int plan_and_run(qcs_handle h, const std::vector<CompiledGate>& cg, int kmax) {
+	const int L0 = low_run_qubits(static_cast<int>(h->n), kmax);
+	const std::vector<PlannedPass> passes = place_gates(cg, kmax, L0, h->scale, h->scale_limit());
 	return h->prec == QCS_FP64 ? run_planned<double>(h, passes, kmax, L0) : run_planned<float>(h, passes, kmax, L0);
 }
 
@@ -915,3 +944,41 @@ void batch_release(qcs_handle h) {
 }
 
 }  // namespace qcs
+
+extern "C" int qcs_plan_gate_passes(uint32_t nqubits, int precision, const qcs_gate* gates, size_t count, uint32_t* pass_ops,
+                                    uint32_t* pass_factors, size_t capacity, size_t* npasses_out) {
+	if ((!gates && count) || !npasses_out || (precision != QCS_FP64 && precision != QCS_FP32) || nqubits < 1 || nqubits > 36)
+		return QCS_INVALID_ARGUMENT;
+	std::vector<qcs::CompiledGate> cg;
+	cg.reserve(count);
+	for (size_t i = 0; i < count; ++i) {
+		const qcs_gate& g = gates[i];
+		if (g.k < 1 || g.k > 3 || g.q0 >= nqubits || (g.k > 1 && g.q1 >= nqubits) || (g.k > 2 && g.q2 >= nqubits))
+			return QCS_INVALID_ARGUMENT;
+		cg.push_back(qcs::compile_gate(g, true));
+	}
+	*npasses_out = 0;
+	const int n = static_cast<int>(nqubits);
+	const int kmax = precision == QCS_FP64 ? qcs::tile_qubits<double>() : qcs::tile_qubits<float>();
+	if (n < kmax + 2 || count < 2) return QCS_OK;  // such lists run one kernel per gate
+	const int L0 = qcs::low_run_qubits(n, kmax);
+	std::complex<double> scale(1.0, 0.0);
+	const std::vector<qcs::PlannedPass> passes = qcs::place_gates(cg, kmax, L0, scale, qcs::scale_limit_of(precision));
+	std::string err;
+	std::vector<qcs::TilePass> tps;
+	if (precision == QCS_FP64) {
+		qcs::PassOps<double> po;
+		if (!qcs::build_pass_ops<double>(n, false, passes, kmax, L0, false, po, err)) return QCS_UNSUPPORTED;
+		tps = std::move(po.tps);
+	} else {
+		qcs::PassOps<float> po;
+		if (!qcs::build_pass_ops<float>(n, false, passes, kmax, L0, false, po, err)) return QCS_UNSUPPORTED;
+		tps = std::move(po.tps);
+	}
+	for (size_t p = 0; p < tps.size() && p < capacity; ++p) {
+		if (pass_ops) pass_ops[p] = tps[p].op_count;
+		if (pass_factors) pass_factors[p] = tps[p].nfactor;
+	}
+	*npasses_out = tps.size();
+	return QCS_OK;
+}

@@ -75,6 +75,10 @@ struct Scratch {
 	size_t pinned_cap = 0;        // in doubles
 };
 
+// the bound on a register's pending global factor: it is folded into the amplitudes once its magnitude
+// leaves [1/limit, limit], so that stored values (amplitude / scale) stay far inside the precision's range
+inline double scale_limit_of(int prec) { return prec == QCS_FP64 ? 1e100 : 1e15; }
+
 }  // namespace qcs
 
 struct qcs_register {
@@ -101,9 +105,7 @@ struct qcs_register {
 	void* prof = nullptr;                  // launch timing records (profile.cu), when enabled
 	std::string err;
 	size_t amp_bytes() const { return prec == QCS_FP64 ? 16 : 8; }
-	// the pending factor is folded into the amplitudes once its magnitude leaves [1/limit, limit], so that
-	// stored values (amplitude / scale) stay far inside the precision's range
-	double scale_limit() const { return prec == QCS_FP64 ? 1e100 : 1e15; }
+	double scale_limit() const { return qcs::scale_limit_of(prec); }
 	size_t state_bytes() const { return static_cast<size_t>(N) * amp_bytes(); }
 	// the largest fused block: the option when set; otherwise 4 for FP32 registers of at least 26 qubits
 	// with the tensor cores on (tensor-core passes of 4-qubit blocks were the fastest greedy partitions

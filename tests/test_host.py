@@ -127,6 +127,66 @@ def test_fusion_plan_covers_every_gate():
     assert counts == sorted(counts, reverse=True)
 
 
+def _restated_gate_passes(layer, kmax: int, low_run: int, window: int = 64) -> int:
+    """the gate-pass planner's packing rule, restated: each pass takes, in order and looking at most
+    `window` gates ahead, every gate whose tile position (its target, unless the gate is diagonal) fits a
+    tile of `kmax` qubits that always holds qubits 0..low_run-1, and which shares no qubit with an earlier
+    gate left waiting"""
+    masks = []
+    for op in layer:
+        g, k = op[0], op[0].getQubitsNumber()
+        touch = 0
+        for q in op[1:1 + k]:
+            touch |= 1 << q
+        masks.append((touch, 0 if g.traits() & L.TRAIT_DIAGONAL else 1 << op[1]))
+    placed, first, passes = [False] * len(masks), 0, 0
+    while True:
+        while first < len(masks) and placed[first]:
+            first += 1
+        if first == len(masks):
+            return passes
+        tmask, waiting, scanned, taken = (1 << low_run) - 1, 0, 0, 0
+        for i in range(first, len(masks)):
+            if scanned >= window:
+                break
+            if placed[i]:
+                continue
+            scanned += 1
+            touch, need = masks[i]
+            if (touch & waiting) == 0 and (bin(tmask | need).count("1") <= kmax or taken == 0):
+                placed[i], taken, tmask = True, taken + 1, tmask | need
+            else:
+                waiting |= touch
+        passes += 1
+
+
+def test_gate_pass_planning():
+    """the pass planner of unfused gate lists (host code, qcs_plan_gate_passes): per layer of the 30-qubit
+    layered circuit it forms exactly the passes of the restated packing rule (FP64: 12-qubit tiles, FP32:
+    13, both holding the 16- or 32-amplitude low run); the diagonal gates outside a pass's tile merge into
+    TileFactor operations only when two or more of them are phases or diagonals"""
+    if not L.LIB_PATH.exists():
+        pytest.skip("libqcs_gpu.so not built")
+    import bench
+    from qcsim_gb300 import costmodel
+    layers = bench.layers_of(circuits.layered_circuit(30, 60, seed=1, p3=0.05), 30)
+    for precision, kmax, low_run in (("fp64", 12, 4), ("fp32", 13, 5)):
+        got = [len(costmodel.gate_passes(30, G.records(layer), precision)) for layer in layers]
+        assert got == [_restated_gate_passes(layer, kmax, low_run) for layer in layers], precision
+    r = np.random.default_rng(5)
+    ops = [(G.HadamardGate(), q) for q in range(12)]
+    for q in range(12, 18):
+        ops.append((G.RzGate(float(r.uniform(0, 2 * np.pi))), q))
+        ops.append((G.PhaseShiftGate(float(r.uniform(0, 2 * np.pi))), q))
+    ops += [(G.ControlledPhaseShiftGate(0.7), 15, 13), (G.ControlledZGate(), 16, 12)]
+    # FP64 tile = qubits 0-11: all 14 diagonal gates merge (the CZ's sign too); FP32 tile = 0-12: the phases
+    # on qubit 12 stay tile operations and the CZ, with its control in the tile, stays its own operation
+    assert costmodel.gate_passes(18, G.records(ops), "fp64") == [(26, 14)]
+    assert costmodel.gate_passes(18, G.records(ops), "fp32") == [(26, 11)]
+    assert costmodel.gate_passes(18, G.records(ops[:13]), "fp64") == [(13, 0)]  # a single non-tile phase
+    assert costmodel.gate_passes(12, G.records(ops[:12]), "fp64") == []  # one kernel per gate below 14 qubits
+
+
 def test_pass_packing_respects_order_and_tiles():
     """the pass planner of the fused path (host code): every block lands in exactly one pass, a block
     never runs before an earlier block it shares a qubit with, every pass fits its tile, and look-ahead
