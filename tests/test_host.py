@@ -90,6 +90,36 @@ def test_c_abi_exports_every_declared_symbol():
     assert declared == set(L.SIGNATURES), declared ^ set(L.SIGNATURES)
 
 
+def test_plain_c_caller(tmp_path):
+    """include/qcs_gpu.h is plain C: tests/c_abi_consumer.c, compiled with gcc as C11 and linked with
+    libqcs_gpu.so, calls the entry points that need no GPU (status strings, the reference's random stream,
+    qcs_create's argument check, the gate-pass and fusion planning) and gets what the Python binding gets"""
+    import shutil
+    import subprocess
+    from qcsim_gb300 import costmodel
+    from qcsim_gb300.register import Rng
+    if not L.LIB_PATH.exists():
+        pytest.skip("libqcs_gpu.so not built")
+    gcc = shutil.which("gcc")
+    if gcc is None:
+        pytest.skip("gcc not found")
+    root = Path(__file__).resolve().parents[1]
+    exe = tmp_path / "c_abi_consumer"
+    subprocess.run([gcc, "-std=c11", "-Wall", "-Wextra", "-Werror", f"-I{root / 'include'}", str(root / "tests" / "c_abi_consumer.c"),
+                    f"-L{L.LIB_PATH.parent}", "-lqcs_gpu", f"-Wl,-rpath,{L.LIB_PATH.parent}", "-lm", "-o", str(exe)],
+                   check=True, capture_output=True, text=True)
+    out = dict(line.split(" ", 1) for line in subprocess.run([str(exe)], check=True, capture_output=True, text=True,
+                                                              timeout=60).stdout.splitlines())
+    assert out["status"] == "invalid argument"
+    assert [float(x) for x in out["uniform"].split()] == Rng(7).uniform(3).tolist()
+    assert int(out["create_zero_qubits"]) == L.QCS_INVALID_ARGUMENT
+    # one pass: the 12 H gates as tile operations, the 4 RZ gates outside the tile as tile factors
+    assert out["plan"].split() == ["0", "1", "16", "4"]
+    ops = [(G.HadamardGate(), q) for q in range(12)] + [(G.RzGate(0.3 + 0.1 * q), q) for q in range(12, 16)]
+    status, nblocks, folded = (int(x) for x in out["fusion"].split())
+    assert status == 0 and folded == 16 and nblocks == len(costmodel.fusion_plan(16, G.records(ops), 4))
+
+
 def test_status_strings_without_gpu():
     if not L.LIB_PATH.exists():
         pytest.skip("libqcs_gpu.so not built")
