@@ -217,6 +217,43 @@ def test_gate_pass_planning():
     assert costmodel.gate_passes(12, G.records(ops[:12]), "fp64") == []  # one kernel per gate below 14 qubits
 
 
+def test_tensor_core_tile_swizzle():
+    """the tensor-core pass's shared-memory swizzle (tc_swizzle in tile.cuh, read from the source): the
+    low-four-bit vectors of the 12 tile bits' offsets are distinct and nonzero and avoid 0011, 1100 and
+    1111, so any 7 of them span GF(2)^4; hence for every block on 4 or 5 tile bits, four of the other bits
+    have independent vectors, and the 16 lanes of a half-warp that differ in those four row bits read 16
+    different 8-byte bank pairs"""
+    import itertools
+    src = (Path(__file__).resolve().parents[1] / "qcsim_gb300" / "csrc" / "tile.cuh").read_text()
+    table = int(re.search(r"\(0x([0-9A-Fa-f]+)ULL >> \(4 \* \(b - 4\)\)\)", src).group(1), 16)
+    vec = [(1 << b) & 15 if b < 4 else (1 << b) & 15 ^ ((table >> (4 * (b - 4))) & 15) for b in range(12)]
+    assert len(set(vec)) == 12 and 0 not in vec and not {0b0011, 0b1100, 0b1111} & set(vec)
+
+    def rank(vs):
+        span = {0}
+        for v in vs:
+            span |= {x ^ v for x in span}
+        return len(span).bit_length() - 1
+
+    assert all(rank(c) == 4 for c in itertools.combinations(vec, 7))
+    for k in (4, 5):
+        for block in itertools.combinations(range(12), k):
+            others = [vec[b] for b in range(12) if b not in block]
+            # the first four independent ones, as the host's row order picks them
+            chosen = []
+            for v in others:
+                if len(chosen) < 4 and rank(chosen + [v]) > len(chosen):
+                    chosen.append(v)
+            lanes = set()
+            for m in range(16):
+                x = 0
+                for r in range(4):
+                    if (m >> r) & 1:
+                        x ^= chosen[r]
+                lanes.add(x)
+            assert len(lanes) == 16, block
+
+
 def test_pass_packing_respects_order_and_tiles():
     """the pass planner of the fused path (host code): every block lands in exactly one pass, a block
     never runs before an earlier block it shares a qubit with, every pass fits its tile, and look-ahead
