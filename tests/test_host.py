@@ -103,9 +103,8 @@ def test_plain_c_caller(tmp_path):
     gcc = shutil.which("gcc")
     if gcc is None:
         pytest.skip("gcc not found")
-    root = Path(__file__).resolve().parents[1]
     exe = tmp_path / "c_abi_consumer"
-    subprocess.run([gcc, "-std=c11", "-Wall", "-Wextra", "-Werror", f"-I{root / 'include'}", str(root / "tests" / "c_abi_consumer.c"),
+    subprocess.run([gcc, "-std=c11", "-Wall", "-Wextra", "-Werror", f"-I{ROOT / 'include'}", str(ROOT / "tests" / "c_abi_consumer.c"),
                     f"-L{L.LIB_PATH.parent}", "-lqcs_gpu", f"-Wl,-rpath,{L.LIB_PATH.parent}", "-lm", "-o", str(exe)],
                    check=True, capture_output=True, text=True)
     out = dict(line.split(" ", 1) for line in subprocess.run([str(exe)], check=True, capture_output=True, text=True,
@@ -224,7 +223,7 @@ def test_tensor_core_tile_swizzle():
     have independent vectors, and the 16 lanes of a half-warp that differ in those four row bits read 16
     different 8-byte bank pairs"""
     import itertools
-    src = (Path(__file__).resolve().parents[1] / "qcsim_gb300" / "csrc" / "tile.cuh").read_text()
+    src = (ROOT / "qcsim_gb300" / "csrc" / "tile.cuh").read_text()
     table = int(re.search(r"\(0x([0-9A-Fa-f]+)ULL >> \(4 \* \(b - 4\)\)\)", src).group(1), 16)
     vec = [(1 << b) & 15 if b < 4 else (1 << b) & 15 ^ ((table >> (4 * (b - 4))) & 15) for b in range(12)]
     assert len(set(vec)) == 12 and 0 not in vec and not {0b0011, 0b1100, 0b1111} & set(vec)
