@@ -58,3 +58,27 @@ def test_fp64_roofline_helper():
     assert r["bound"] == "fp64" and r["fp_ops_per_launch"] == pytest.approx(2.0e10)
     assert r["achieved"] == pytest.approx(8.0e10 / 0.1 / 1e12)
     assert r["peak"] == pytest.approx(0.6) and r["frac"] == pytest.approx(r["achieved"] / 0.6)
+
+
+def test_parity_helpers():
+    """the parity leg's helpers: the identity rate of two shot histograms of the same uniforms, the count
+    of uniforms within eps of a cumulative-table entry (chunked as on a 30-qubit state), the layer split
+    of the layered circuit, and the oracle's max amplitude difference"""
+    import numpy as np
+    import bench
+    from qcsim_gb300 import circuits
+    assert bench.shot_identity({1: 3, 2: 1}, {1: 3, 2: 1}, 4) == 1.0
+    assert bench.shot_identity({1: 3, 2: 1}, {1: 2, 3: 2}, 4) == 0.5
+    assert bench.shot_identity({}, {}, 0) == 1.0
+    state = np.sqrt(np.array([0.25, 0.25, 0.5], dtype=np.complex128))  # cumulative table 0.25, 0.5, 1.0
+    probs = np.array([0.1, 0.25 + 1e-14, 0.5 - 1e-13, 0.75, 1.0 - 1e-15])
+    for chunk in (1, 2, 1 << 24):
+        assert bench.shots_near_boundary(state, probs, 1e-12, chunk=chunk) == 3
+    ops = circuits.layered_circuit(12, 5, seed=2, p3=0.05)
+    layers = bench.layers_of(ops, 12)
+    assert len(layers) == 5 and sum(map(len, layers)) == len(ops)
+    assert all(sum(type(o[0]).__name__ == "CNOTGate" for o in layer) == 6 for layer in layers)
+    from oracle import bind
+    bind.build_oracle()
+    a = np.array([1 + 2j, 3 - 1j, 0.5j])
+    assert bench.max_abs_diff(a, a + np.array([0, 1e-9, 0])) == pytest.approx(1e-9)
